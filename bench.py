@@ -1,0 +1,327 @@
+"""Benchmark: RK4 DOF-stage updates/s of the LDG Navier-Stokes RHS on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--nx 64] [--p 4]
+
+One "step" is one classical RK4 time step (four RHS stages) of the periodic
+Taylor-Green vortex, Re=1600, Ma=0.1, on an nx^3 hex mesh of order p (default
+64^3, p=4: 262,144 elements, 32.8M nodal DOFs x 5 variables, 1.31 GB of
+state, larger than L2).  The metric counts nodal DOF-stage updates:
+(p+1)^3 * nE * 4 per step.
+
+  value  device-resident: ldg_step on the solver's stream, CUDA events.
+  e2e    through the C ABI with host buffers: every step uploads the state
+         from pinned host memory (ldg_set_state), advances one RK4 step and
+         reads the new state back (ldg_get_state).
+
+--impl reference times the CPU oracle (the restatement of the reference's
+dense BLAS/LAPACK path, with OpenBLAS when available and all host threads)
+on a bounded sample of the same workload (smaller mesh, same order).
+
+Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "local-dg_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "RK4 DOF-stage updates/s (FP64 LDG Navier-Stokes RHS, Taylor-Green)"
+UNIT = "DOF-stage/s"
+
+# Algorithmic HBM bytes per nodal DOF-stage (FP64): read U, write q (15),
+# read U, read q, write k: 8*(5+15+5+15+5) = 360 B.  Split per pass:
+BYTES_GRAD = 8 * (5 + 15)        # read U, write q
+BYTES_RHS = 8 * (5 + 15 + 5)     # read U, read q, write k / next stage
+
+
+def fp64_flops_per_element_stage(N: int) -> float:
+    """FP64 floating-point operations the sum-factorised kernels perform per
+    element and RK stage (counted from the kernels; FMA = 2).  Divisions and
+    square roots are counted as one operation each here."""
+    n, nf = N ** 3, N ** 2
+    grad = (3 * 5 * 2 * N * n          # A_l contractions of U
+            + 3 * 5 * 4 * n            # lifts (2 FMA) + scale
+            + 3 * 15 * 2 * N * nf)     # minus-face traces of q
+    vol = n * (13 + 5 * 3 + 9 * 3 + 3 * 9 + 20 + 3 * 12 + 15)  # Euler + viscous flux per point
+    face = 6 * nf * (110 + 60)         # Roe + one viscous column per face point
+    rhs = (vol + face
+           + 3 * 5 * 2 * N * n         # A_l contractions of F
+           + 6 * 5 * 2 * n             # face lifts
+           + 5 * 4 * n                 # RK update
+           + 6 * 5 * 2 * N * nf)       # traces of the next stage
+    return float(grad + rhs)
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline(p: int, seconds_budget: float = 20.0, steps: int | None = None):
+    """The oracle on the host cores: bounded sample of the workload."""
+    import numpy as np
+    import oracle
+    threads = os.cpu_count() or 1
+    blas = oracle.find_openblas()
+    nx = 16 if p >= 4 else 20
+    o = oracle.Oracle(nx, p, steps=1, threads=threads, openblas=blas)
+    u = o.initial_condition()
+    u, _ = o.step(u, 1)  # warm-up
+    n_steps = 0
+    t0 = time.perf_counter()
+    while True:
+        u, _ = o.step(u, 1)
+        n_steps += 1
+        el = time.perf_counter() - t0
+        if steps is not None and n_steps >= steps:
+            break
+        if steps is None and (el > seconds_budget or n_steps >= 50):
+            break
+    value = o.dofs * o.nE * 4 * n_steps / el
+    assert np.all(np.isfinite(u))
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{nx}^3 p={p} Taylor-Green, {n_steps} RK4 steps, "
+                      f"{'OpenBLAS' if blas else 'C loops'} + OpenMP x{threads}",
+            "seconds": el}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    import numpy as np
+    threads = os.cpu_count() or 1
+    blas = oracle.find_openblas()
+    nx = 16 if args.p >= 4 else 20
+    o = oracle.Oracle(nx, args.p, steps=1, threads=threads, openblas=blas)
+    u = o.initial_condition()
+    for _ in range(args.warmup):
+        u, _ = o.step(u, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        u, _ = o.step(u, 1)
+    el = time.perf_counter() - t0
+    assert np.all(np.isfinite(u))
+    value = o.dofs * o.nE * 4 * args.steps / el
+    sample = (f"{nx}^3 p={args.p} Taylor-Green (per-element work of the {args.nx}^3 p={args.p} "
+              f"workload), {'OpenBLAS' if blas else 'C loops'} + OpenMP x{threads}")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (Taylor-Green initial condition)",
+        "config": {"workload": f"tgv_{args.nx}^3_p{args.p}_fp64", "nx": args.nx, "p": args.p,
+                   "sample_nx": nx},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import ldg
+
+    ws, rank, local = dist_env()
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    ldg.load()
+    K, W = args.steps, args.warmup
+    s = ldg.Solver(args.p, args.nx, steps=max(K + W, 1) * 3 + 8, device=dev, check_finite=True)
+    n_per_step = s.dofs * s.nE * 4
+    stream = torch.cuda.ExternalStream(s.stream, device=dev)
+
+    # ---- device-resident timed region
+    for _ in range(W):
+        s.step(1)
+    s.synchronize()
+    s.enable_kernel_timing(True)
+    s.kernel_times(reset=True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        s.step(K)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kt = s.kernel_times(reset=True)
+    s.enable_kernel_timing(False)
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * n_per_step * K / (ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers
+    state_bytes = s.nE * 5 * s.dofs * 8
+    host = torch.empty(s.shape, dtype=torch.float64, pin_memory=True).numpy()
+    s.get_state(host)
+    s.step(1)  # warm the path
+    s.synchronize()
+    Ke = max(1, min(K, 5))
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        s.set_state(host)
+        s.step(1)
+        s.get_state(host)
+    e2e_s = time.perf_counter() - t0
+    assert np.all(np.isfinite(host))
+    e2e = {"value": ws * n_per_step * Ke / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes}
+
+    # ---- roofline of the dominant kernel (live event timings above)
+    hbm_peak, peak_kind = read_peaks()
+    dom = "rhs" if kt["rhs"][0] >= kt["grad"][0] else "grad"
+    dom_ms, dom_n = kt[dom]
+    avg_s = dom_ms * 1e-3 / max(dom_n, 1)
+    per_dof = BYTES_RHS if dom == "rhs" else BYTES_GRAD
+    alg_bytes = per_dof * s.dofs * s.nE
+    achieved = alg_bytes / avg_s / 1e9
+    N = args.p + 1
+    fp64_peak = ldg.probe_fp64_peak(dev)
+    flops_step = fp64_flops_per_element_stage(N) * s.nE * 4
+    fp64_achieved = flops_step * K / (ms * 1e-3) / 1e12
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None,
+                "kernel": f"k_rhs<{N}>" if dom == "rhs" else f"k_grad<{N}>",
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "binding_roof": {"pipe": "fp64", "achieved_tflops": fp64_achieved,
+                                 "peak_tflops": fp64_peak, "frac": fp64_achieved / fp64_peak,
+                                 "peak_source": "measured (ldg_probe_fp64_peak FMA chain)",
+                                 "flops_per_dof_stage": fp64_flops_per_element_stage(N) / N ** 3}}
+    kernel_ms = {k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1)} for k, v in kt.items()}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (Taylor-Green initial condition, Re=1600, Ma=0.1)",
+        "config": {"workload": f"tgv_{args.nx}^3_p{args.p}_fp64", "nx": args.nx, "p": args.p,
+                   "elements": s.nE, "dofs_per_element": s.dofs, "precision": "fp64",
+                   "l2": "inputs larger than L2 (state 1.31 GB at 64^3 p4)" if s.nE * s.dofs * 40 > 129e6
+                   else "inputs smaller than L2", "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "e2e": e2e,
+        "roofline": roofline,
+        "kernels": kernel_ms,
+        "gpu_launches": int(kt["grad"][1] + kt["rhs"][1] + kt["reduce"][1]),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.p)
+    s.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=64)
+    ap.add_argument("--p", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

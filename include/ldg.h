@@ -1,0 +1,173 @@
+/*
+ * ldg.h -- C ABI of the GB300 (sm_103a) LDG Navier-Stokes right-hand side.
+ *
+ * This is the drop-in boundary for the hot path of Local-DG: the RK4
+ * time step of the Local Discontinuous Galerkin discretisation of 3-D
+ * compressible Navier-Stokes on a periodic uniform hex mesh.  The
+ * reference has no FFI; its boundary is the C++ class Solver
+ * (solver.h:20-115), whose constructor Solver(p, dtSnaps, tf, L, mesh)
+ * (solver.cpp:7-71) and dgTimeStep() (solver.cpp:295-453) drive the
+ * internal seam rk4UpdateCurr/rk4Rhs (solver.h:76-79).  Each entry point
+ * below names the reference interface it replaces.  include/ldg_solver.hpp
+ * rebuilds the Solver/Mesh classes on top of these calls.
+ *
+ * Conventions
+ *  - Every call returns an int status: LDG_OK (0) or a negative LDG_ERR_*.
+ *    ldg_error_string() names it; ldg_last_error_message() gives detail.
+ *  - State arrays use the reference layout: darray u(dofs, 5, nElements),
+ *    column major (solver.cpp:62), i.e. element-major blocks of 5 variables
+ *    (rho, rho*u, rho*v, rho*w, rho*E; solver.cpp:217-229), each a block of
+ *    dofs = (p+1)^3 nodal values, node = ix + N*iy + N*N*iz, N = p+1.
+ *  - Elements are numbered e = ix + nx*(iy + ny*iz) (mesh.cpp:162) on the
+ *    periodic cube [-pi L, pi L]^3.
+ *  - Pointers are host pointers unless the call takes `where` =
+ *    LDG_DEVICE, in which case they are device pointers on the solver's GPU.
+ *  - A handle owns its device buffers and one CUDA stream; calls on one
+ *    handle are not thread safe (like the reference Solver).  All calls
+ *    are stream ordered; calls that return host data synchronise.
+ */
+#ifndef LDG_H
+#define LDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LDG_ABI_VERSION 1
+
+/* status codes */
+#define LDG_OK 0
+#define LDG_ERR_INVALID -1     /* bad argument or configuration            */
+#define LDG_ERR_CUDA -2        /* a CUDA call failed                       */
+#define LDG_ERR_NOMEM -3       /* device or host allocation failed         */
+#define LDG_ERR_NONFINITE -4   /* NaN/Inf found in the state after a step  */
+#define LDG_ERR_UNSUPPORTED -5 /* order or mode not built                  */
+#define LDG_ERR_NODEVICE -6    /* no CUDA device visible                   */
+
+/* where a pointer lives */
+#define LDG_HOST 0
+#define LDG_DEVICE 1
+
+/* arithmetic of the RHS */
+#define LDG_FP64 0  /* every operation in FP64 */
+
+typedef struct ldg_config {
+  int p;            /* polynomial order, 1..7 (Solver ctor _p)           */
+  int nx, ny, nz;   /* elements per direction, each >= 3 (mesh.cpp:102) */
+  double L;         /* domain [-pi L, pi L]^3 (driver.cpp:26-31)        */
+  double tf;        /* final time (Solver ctor _tf)                      */
+  int dt_snaps;     /* snapshot cadence (Solver ctor _dtSnaps); 0 = none */
+  double Re;        /* Reynolds number (solver.cpp:30), default 1600     */
+  double Pr;        /* Prandtl number (solver.cpp:31), default 0.71      */
+  double gamma;     /* ratio of specific heats (solver.cpp:32), 1.4      */
+  double Ma;        /* Mach number (solver.cpp:33), default 0.1          */
+  double cfl;       /* dt = cfl*min(dx)/(V0(2p+1)) (solver.cpp:47), 0.01 */
+  int precision;    /* LDG_FP64                                          */
+  int device;       /* CUDA device ordinal                               */
+  int check_finite; /* nonzero: ldg_step scans the state for NaN/Inf     */
+  int use_box;      /* 0: domain [-pi L, pi L]^3 (driver.cpp:28-31);
+                       1: [box_lo, box_hi] (Mesh botLeft/topRight,
+                       mesh.cpp:51-151); periodic either way             */
+  double box_lo[3], box_hi[3];
+  int reserved[8];
+} ldg_config;
+
+typedef struct ldg_info {
+  int p, dofs, nf;          /* (p+1)^3 nodes, (p+1)^2 face points       */
+  int nx, ny, nz, nelements;
+  double dt;                /* time step after the tf adjustment         */
+  long long timesteps;      /* ceil(tf/dt) (solver.cpp:51-52)            */
+  long long step;           /* RK4 steps taken so far                    */
+  double time;              /* step * dt                                 */
+  size_t device_bytes;      /* device memory held by the handle          */
+  int precision;
+} ldg_info;
+
+typedef struct ldg_solver ldg_solver;
+
+/* Fills the reference defaults (solver.cpp:30-52; driver.cpp:26-39). */
+int ldg_config_default(ldg_config* cfg);
+
+/* Replaces Solver::Solver(p, dtSnaps, tf, L, mesh) (solver.cpp:7-71):
+ * physics, CFL time step, operators, and the Taylor-Green initial
+ * condition (solver.cpp:194-236) as the current state. */
+int ldg_create(const ldg_config* cfg, ldg_solver** out);
+
+/* Frees the handle and every device buffer it owns. */
+int ldg_destroy(ldg_solver* s);
+
+int ldg_get_info(const ldg_solver* s, ldg_info* info);
+
+/* Sets / reads the solver state Solver::u (solver.h:44) in the reference
+ * layout; where = LDG_HOST or LDG_DEVICE. */
+int ldg_set_state(ldg_solver* s, const double* u, int where);
+int ldg_get_state(ldg_solver* s, double* u, int where);
+
+/* Resets the state to the Taylor-Green vortex (solver.cpp:194-236) and the
+ * step counter to 0. */
+int ldg_set_initial_condition(ldg_solver* s);
+
+/* One right-hand side k = rhs(uCurr), both in the reference layout: the
+ * seam Solver::rk4Rhs(uCurr, ..., ks, istage) (solver.h:77-79,
+ * solver.cpp:486-535) for one stage.  Does not change the state. */
+int ldg_rhs(ldg_solver* s, const double* u_curr, double* k, int where);
+
+/* Advances nsteps classical RK4 steps (the loop body of
+ * Solver::dgTimeStep, solver.cpp:410-440: stage combine rk4UpdateCurr
+ * solver.cpp:458-480, rk4Rhs, accumulation u += dt*b_s*k_s in stage order)
+ * and records computeKE (solver.cpp:1007-1034) after every step. */
+int ldg_step(ldg_solver* s, int nsteps);
+
+/* Replaces Solver::dgTimeStep() (solver.cpp:295-453): all remaining steps
+ * to tf.  No CSV output (io.cpp is out of scope); the KE series is kept. */
+int ldg_time_step(ldg_solver* s);
+
+/* Diagnostics of the current state:
+ *   ke_ref    computeKE exactly as the reference (nodal values weighted by
+ *             Gauss weights, solver.cpp:1021-1031);
+ *   ke        kinetic energy by Gauss quadrature of |m|^2/(2 rho);
+ *   enstrophy quadrature of rho |curl v|^2 / 2 from the LDG gradient;
+ * each normalised by rho0 (2 pi L)^3.  Any pointer may be NULL. */
+int ldg_diagnostics(ldg_solver* s, double* ke_ref, double* ke, double* enstrophy);
+
+/* KE series recorded by ldg_step (computeKE after each step, as
+ * dgTimeStep's kes, solver.cpp:437), and the dissipation rate
+ * -(KE_n - KE_{n-2})/(2 dt) (solver.cpp:438-440).  *count receives the
+ * number of entries available; at most max are copied. */
+int ldg_ke_history(ldg_solver* s, double* ke, int max, int* count);
+int ldg_ke_dissipation(ldg_solver* s, double* eps, int max, int* count);
+
+/* Waits for all work queued on the handle's stream. */
+int ldg_synchronize(ldg_solver* s);
+
+/* The handle's CUDA stream (a cudaStream_t) so callers can order their
+ * own work against it. */
+void* ldg_stream(ldg_solver* s);
+
+/* Per-kernel device time, for roofline reporting.  enable != 0 brackets
+ * every kernel that ldg_step launches with CUDA events on the handle's
+ * stream; ldg_kernel_times then returns, per kernel class, the summed
+ * milliseconds and launch counts since the last reset (reset != 0 clears
+ * them).  Classes: 0 gradient pass, 1 RHS+RK pass, 2 KE reduction.
+ * (No reference counterpart: the reference only prints wall-clock,
+ * solver.cpp:344-371.) */
+#define LDG_KERNEL_CLASSES 3
+int ldg_enable_kernel_timing(ldg_solver* s, int enable);
+int ldg_kernel_times(ldg_solver* s, double* ms, long long* launches, int max_classes, int reset);
+
+/* Measures the FP64 FMA rate of the device (TFLOP/s, 2 flops per FMA) with
+ * a register-resident FMA chain; the roofline denominator for the FP64
+ * kernels.  (No reference counterpart.) */
+int ldg_probe_fp64_peak(int device, double* tflops);
+
+const char* ldg_error_string(int status);
+const char* ldg_last_error_message(void);
+int ldg_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LDG_H */

@@ -1,0 +1,327 @@
+"""Python front end of libldg_gb300.so (the C ABI in include/ldg.h).
+
+Mirrors the reference's Solver interface (Local-DG solver.h:109-113):
+``Solver(p, dt_snaps, tf, L, mesh)`` plus ``dg_time_step()``, and exposes the
+seam the GPU path replaces: ``rhs(u)`` (Solver::rk4Rhs, solver.cpp:486-535)
+and ``step(n)`` (the RK4 loop body of Solver::dgTimeStep,
+solver.cpp:410-440).  State arrays use the reference layout
+u(node, var, elem) column major == numpy C-order (nE, 5, dofs).
+
+The library is built in-tree by :func:`build` (nvcc, sm_103a).  There is no
+CPU fallback: every call goes through the CUDA library, and loading fails
+loudly if it is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libldg_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
+SOURCES = ["ldg_capi.cu", "ldg_ops.cpp"]
+
+LDG_OK = 0
+LDG_HOST = 0
+LDG_DEVICE = 1
+LDG_FP64 = 0
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compiles libldg_gb300.so for sm_103a (translation units in parallel)."""
+    if not force and not _stale():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        if src.endswith(".cpp"):
+            cmd = [nvcc, "-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-c",
+                   os.path.join(CSRC, src), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
+        if verbose:
+            sys.stderr.write(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB + ".tmp"
+    r = subprocess.run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class LdgConfig(ctypes.Structure):
+    _fields_ = [
+        ("p", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("L", ctypes.c_double), ("tf", ctypes.c_double), ("dt_snaps", ctypes.c_int),
+        ("Re", ctypes.c_double), ("Pr", ctypes.c_double), ("gamma", ctypes.c_double),
+        ("Ma", ctypes.c_double), ("cfl", ctypes.c_double), ("precision", ctypes.c_int),
+        ("device", ctypes.c_int), ("check_finite", ctypes.c_int), ("use_box", ctypes.c_int),
+        ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3),
+        ("reserved", ctypes.c_int * 8),
+    ]
+
+
+class LdgInfo(ctypes.Structure):
+    _fields_ = [
+        ("p", ctypes.c_int), ("dofs", ctypes.c_int), ("nf", ctypes.c_int),
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("nelements", ctypes.c_int),
+        ("dt", ctypes.c_double), ("timesteps", ctypes.c_longlong), ("step", ctypes.c_longlong),
+        ("time", ctypes.c_double), ("device_bytes", ctypes.c_size_t), ("precision", ctypes.c_int),
+    ]
+
+
+# Every symbol include/ldg.h declares, with its ctypes signature.
+_vp, _i, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+SIGNATURES = {
+    "ldg_config_default": (_i, [ctypes.POINTER(LdgConfig)]),
+    "ldg_create": (_i, [ctypes.POINTER(LdgConfig), ctypes.POINTER(_vp)]),
+    "ldg_destroy": (_i, [_vp]),
+    "ldg_get_info": (_i, [_vp, ctypes.POINTER(LdgInfo)]),
+    "ldg_set_state": (_i, [_vp, _vp, _i]),
+    "ldg_get_state": (_i, [_vp, _vp, _i]),
+    "ldg_set_initial_condition": (_i, [_vp]),
+    "ldg_rhs": (_i, [_vp, _vp, _vp, _i]),
+    "ldg_step": (_i, [_vp, _i]),
+    "ldg_time_step": (_i, [_vp]),
+    "ldg_diagnostics": (_i, [_vp, _dp, _dp, _dp]),
+    "ldg_ke_history": (_i, [_vp, _dp, _i, _ip]),
+    "ldg_ke_dissipation": (_i, [_vp, _dp, _i, _ip]),
+    "ldg_synchronize": (_i, [_vp]),
+    "ldg_stream": (_vp, [_vp]),
+    "ldg_enable_kernel_timing": (_i, [_vp, _i]),
+    "ldg_kernel_times": (_i, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _i, _i]),
+    "ldg_probe_fp64_peak": (_i, [_i, _dp]),
+    "ldg_error_string": (ctypes.c_char_p, [_i]),
+    "ldg_last_error_message": (ctypes.c_char_p, []),
+    "ldg_abi_version": (_i, []),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads the CUDA library (building it first if needed)."""
+    global _lib
+    if _lib is None:
+        path = path or build()
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def probe_fp64_peak(device: int = 0) -> float:
+    """Measured FP64 FMA rate of the device in TFLOP/s."""
+    out = ctypes.c_double()
+    _check(load().ldg_probe_fp64_peak(device, ctypes.byref(out)), "ldg_probe_fp64_peak")
+    return out.value
+
+
+class LdgError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        L = load()
+        super().__init__(f"{where}: {L.ldg_error_string(status).decode()} "
+                         f"({L.ldg_last_error_message().decode()})")
+        self.status = status
+
+
+def _check(status: int, where: str):
+    if status != LDG_OK:
+        raise LdgError(status, where)
+
+
+def tf_for_steps(nx: int, p: int, L: float, steps: int, cfl: float = 0.01) -> float:
+    """Final time whose CFL step count (solver.cpp:47-52) is exactly steps."""
+    size = math.pi * L
+    dt0 = cfl * ((size - (-size)) / nx) / (1.0 * (2 * p + 1))
+    tf = steps * dt0
+    while math.ceil(tf / dt0) > steps:
+        tf = float(np.nextafter(tf, 0.0))
+    return float(tf)
+
+
+def _arg(a, where_hint=None):
+    """(pointer, where, keepalive) for a numpy array or a CUDA torch tensor."""
+    if isinstance(a, np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        return a.ctypes.data, LDG_HOST, a
+    t = a
+    if getattr(t, "is_cuda", False):
+        assert t.is_contiguous() and str(t.dtype) == "torch.float64"
+        return t.data_ptr(), LDG_DEVICE, t
+    raise TypeError("expected a numpy array or a CUDA float64 torch tensor")
+
+
+class Solver:
+    """GPU LDG solver on an nx x ny x nz periodic hex mesh of order p."""
+
+    def __init__(self, p: int, nx: int, ny: int | None = None, nz: int | None = None, *, L: float = 1.0,
+                 tf: float | None = None, steps: int | None = None, Re: float = 1600.0, Pr: float = 0.71,
+                 gamma: float = 1.4, Ma: float = 0.1, cfl: float = 0.01, device: int = 0,
+                 check_finite: bool = True, dt_snaps: int = 0, box=None):
+        L_ = load()
+        cfg = LdgConfig()
+        _check(L_.ldg_config_default(ctypes.byref(cfg)), "ldg_config_default")
+        cfg.p, cfg.nx = p, nx
+        cfg.ny = ny if ny is not None else nx
+        cfg.nz = nz if nz is not None else nx
+        cfg.L = L
+        if tf is None:
+            tf = tf_for_steps(max(cfg.nx, cfg.ny, cfg.nz), p, L, steps if steps else 1, cfl)
+        cfg.tf = tf
+        cfg.Re, cfg.Pr, cfg.gamma, cfg.Ma, cfg.cfl = Re, Pr, gamma, Ma, cfl
+        cfg.device = device
+        cfg.check_finite = 1 if check_finite else 0
+        cfg.dt_snaps = dt_snaps
+        if box is not None:
+            cfg.use_box = 1
+            for l in range(3):
+                cfg.box_lo[l], cfg.box_hi[l] = box[0][l], box[1][l]
+        h = ctypes.c_void_p()
+        _check(L_.ldg_create(ctypes.byref(cfg), ctypes.byref(h)), "ldg_create")
+        self._h = h
+        self.cfg = cfg
+        info = self.info()
+        self.p, self.dofs, self.nE, self.dt = p, info.dofs, info.nelements, info.dt
+        self.timesteps = info.timesteps
+        self.shape = (self.nE, 5, self.dofs)
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ldg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def info(self) -> LdgInfo:
+        info = LdgInfo()
+        _check(load().ldg_get_info(self._h, ctypes.byref(info)), "ldg_get_info")
+        return info
+
+    def set_state(self, u) -> None:
+        ptr, where, keep = _arg(u)
+        _check(load().ldg_set_state(self._h, ptr, where), "ldg_set_state")
+        if where == LDG_DEVICE:
+            self.synchronize()
+        del keep
+
+    def get_state(self, out=None):
+        if out is None:
+            out = np.empty(self.shape)
+        ptr, where, keep = _arg(out)
+        _check(load().ldg_get_state(self._h, ptr, where), "ldg_get_state")
+        if where == LDG_DEVICE:
+            self.synchronize()
+        return keep if where == LDG_DEVICE else out
+
+    def set_initial_condition(self) -> None:
+        _check(load().ldg_set_initial_condition(self._h), "ldg_set_initial_condition")
+
+    def rhs(self, u, out=None):
+        ptr, where, keep = _arg(u)
+        if out is None:
+            out = np.empty(self.shape) if where == LDG_HOST else None
+            if out is None:
+                import torch
+                out = torch.empty_like(keep)
+        optr, owhere, okeep = _arg(out)
+        assert owhere == where, "input and output must live on the same side"
+        _check(load().ldg_rhs(self._h, ptr, optr, where), "ldg_rhs")
+        if where == LDG_DEVICE:
+            self.synchronize()
+        return out
+
+    def step(self, nsteps: int = 1) -> None:
+        _check(load().ldg_step(self._h, nsteps), "ldg_step")
+
+    def dg_time_step(self) -> None:
+        _check(load().ldg_time_step(self._h), "ldg_time_step")
+
+    def diagnostics(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(load().ldg_diagnostics(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "ldg_diagnostics")
+        return a.value, b.value, c.value
+
+    def ke_history(self) -> np.ndarray:
+        cnt = ctypes.c_int()
+        _check(load().ldg_ke_history(self._h, None, 0, ctypes.byref(cnt)), "ldg_ke_history")
+        out = np.zeros(cnt.value)
+        if cnt.value:
+            _check(load().ldg_ke_history(self._h, out.ctypes.data_as(_dp), cnt.value, ctypes.byref(cnt)),
+                   "ldg_ke_history")
+        return out
+
+    def ke_dissipation(self) -> np.ndarray:
+        cnt = ctypes.c_int()
+        _check(load().ldg_ke_dissipation(self._h, None, 0, ctypes.byref(cnt)), "ldg_ke_dissipation")
+        out = np.zeros(cnt.value)
+        if cnt.value:
+            _check(load().ldg_ke_dissipation(self._h, out.ctypes.data_as(_dp), cnt.value, ctypes.byref(cnt)),
+                   "ldg_ke_dissipation")
+        return out
+
+    def synchronize(self) -> None:
+        _check(load().ldg_synchronize(self._h), "ldg_synchronize")
+
+    def enable_kernel_timing(self, enable: bool = True) -> None:
+        _check(load().ldg_enable_kernel_timing(self._h, 1 if enable else 0), "ldg_enable_kernel_timing")
+
+    def kernel_times(self, reset: bool = False):
+        """{class: (total_ms, launches)} for 'grad', 'rhs', 'reduce'."""
+        ms = (ctypes.c_double * 3)()
+        n = (ctypes.c_longlong * 3)()
+        _check(load().ldg_kernel_times(self._h, ms, n, 3, 1 if reset else 0), "ldg_kernel_times")
+        return {name: (ms[i], n[i]) for i, name in enumerate(("grad", "rhs", "reduce"))}
+
+    @property
+    def stream(self) -> int:
+        return load().ldg_stream(self._h)

@@ -1,0 +1,827 @@
+/*
+ * ldg_oracle.c -- CPU restatement of the Local-DG reference hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle: tests/, the smoke check in
+ * __graft_entry__.py and bench.py's CPU-baseline leg call it as the checker
+ * or as the timed CPU baseline.  The product path (local-dg_gb300/) never
+ * links, loads or falls back to it.
+ *
+ * It restates, in plain C with the reference's dense-operator structure,
+ * the RK4 right-hand side of the LDG discretisation of 3-D compressible
+ * Navier-Stokes on a periodic uniform hex mesh (Local-DG solver.cpp).  Each
+ * function names the reference lines it follows.  Layout is the reference's
+ * column-major darray: u(node, var, elem), node = ix + N*iy + N*N*iz.
+ *
+ * Dense GEMMs and the mass-matrix LDL^T solve run on project-written loops
+ * (OpenMP over columns).  Optionally ldgo_use_openblas() routes them to an
+ * OpenBLAS shared library (the same BLAS/LAPACK calls the reference makes,
+ * solver.cpp:500-506,532-533,560-572,736-738,859-861), which is how the CPU
+ * baseline reproduces the reference's threaded-BLAS cost profile.
+ *
+ * Parity pin: outputs are checked against golden vectors produced by the
+ * unmodified reference sources (oracle/build_ref.sh + oracle/ref_driver.cpp)
+ * in tests/golden/.
+ */
+#include <dlfcn.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+#define NS 5    /* conserved variables (solver.cpp:61) */
+#define DIM 3
+#define NF 6    /* faces per element, ordered -x,+x,-y,+y,-z,+z (mesh.h:143-147) */
+
+typedef void (*dgemm_fn)(int, int, int, int, int, int, double, const double*, int, const double*,
+                         int, double, double*, int);
+typedef int (*dsytrf_fn)(int, char, int, double*, int, int*);
+typedef int (*dsytrs_fn)(int, char, int, int, const double*, int, const int*, double*, int);
+typedef void (*setthreads_fn)(int);
+
+typedef struct ldgo {
+  int p, N, n, nf, nx, ny, nz, nE;
+  double L, minDX, minDY, minDZ, alpha[DIM], J;
+  /* physics (solver.cpp:30-43) */
+  double Re, Pr, gamma, M0, R, rho0, V0, c0, p0, T0;
+  double dt;
+  long timesteps;
+  /* operators (solver.cpp:74-192) */
+  double *Interp2D; /* nf x nf   */
+  double *Interp3D; /* n x n     */
+  double *Mel;      /* n x n, factored in place */
+  int *Mipiv;
+  double *Sels;     /* n x n x 3 */
+  double *Kels;     /* n x n x 3 */
+  double *Kels2D;   /* nf x nf x 3 */
+  double *wQ3;      /* n */
+  int *efToN;       /* nf x 6 */
+  int *eToE;        /* 6 x nE, periodic neighbour (ghost slots resolved) */
+  /* work arrays (solver.cpp:318-325) */
+  double *uCurr, *uInterp2D, *uInterp3D, *ks, *Dus, *DuInterp2D, *DuInterp3D, *onFaces, *flx;
+  /* optional OpenBLAS */
+  void *blas;
+  dgemm_fn dgemm;
+  dsytrf_fn dsytrf;
+  dsytrs_fn dsytrs;
+  int threads;
+} ldgo;
+
+/* ---------------------------------------------------------------- BLAS-like */
+
+/* C = alpha*op(A)*B + beta*C, column-major; op(A) = A (ta=0) or A^T (ta=1). */
+static void gemm(const ldgo* o, int ta, int M, int Ncol, int K, double alpha, const double* A,
+                 int lda, const double* B, int ldb, double beta, double* C, int ldc) {
+  if (o && o->dgemm) {
+    o->dgemm(102, ta ? 112 : 111, 111, M, Ncol, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    return;
+  }
+  long j;
+#pragma omp parallel for schedule(static) if (Ncol > 64)
+  for (j = 0; j < Ncol; ++j) {
+    double* c = C + (long)j * ldc;
+    const double* b = B + (long)j * ldb;
+    if (beta == 0.0) {
+      for (int i = 0; i < M; ++i) c[i] = 0.0;
+    } else if (beta != 1.0) {
+      for (int i = 0; i < M; ++i) c[i] *= beta;
+    }
+    if (!ta) {
+      for (int k = 0; k < K; ++k) {
+        double bk = alpha * b[k];
+        const double* a = A + (long)k * lda;
+        for (int i = 0; i < M; ++i) c[i] += a[i] * bk;
+      }
+    } else {
+      for (int i = 0; i < M; ++i) {
+        const double* a = A + (long)i * lda;
+        double s = 0.0;
+        for (int k = 0; k < K; ++k) s += a[k] * b[k];
+        c[i] += alpha * s;
+      }
+    }
+  }
+}
+
+/* LU with partial pivoting; solves A X = B in place (B: n x nrhs).  Used for
+ * the Vandermonde inverses the reference obtains from LAPACKE_dgesv
+ * (solver.cpp:109-111, dgMath.cpp:522-524,560-562,600-602). */
+static int lu_solve(int n, double* A, int nrhs, double* B) {
+  int* piv = (int*)malloc(sizeof(int) * n);
+  for (int k = 0; k < n; ++k) {
+    int pr = k;
+    double mx = fabs(A[k + k * n]);
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[i + k * n]) > mx) { mx = fabs(A[i + k * n]); pr = i; }
+    piv[k] = pr;
+    if (mx == 0.0) { free(piv); return -1; }
+    if (pr != k) {
+      for (int j = 0; j < n; ++j) { double t = A[k + j * n]; A[k + j * n] = A[pr + j * n]; A[pr + j * n] = t; }
+      for (int j = 0; j < nrhs; ++j) { double t = B[k + j * n]; B[k + j * n] = B[pr + j * n]; B[pr + j * n] = t; }
+    }
+    for (int i = k + 1; i < n; ++i) {
+      double f = A[i + k * n] / A[k + k * n];
+      A[i + k * n] = f;
+      for (int j = k + 1; j < n; ++j) A[i + j * n] -= f * A[k + j * n];
+      for (int j = 0; j < nrhs; ++j) B[i + j * n] -= f * B[k + j * n];
+    }
+  }
+  for (int j = 0; j < nrhs; ++j) {
+    double* b = B + (long)j * n;
+    for (int i = n - 1; i >= 0; --i) {
+      double s = b[i];
+      for (int k = i + 1; k < n; ++k) s -= A[i + k * n] * b[k];
+      b[i] = s / A[i + i * n];
+    }
+  }
+  free(piv);
+  return 0;
+}
+
+/* Mass-matrix factorisation.  The reference uses Bunch-Kaufman LDL^T
+ * (LAPACKE_dsytrf 'U', solver.cpp:155-156).  Mel is symmetric positive
+ * definite, so the restatement uses LDL^T without pivoting, M = U^T D U
+ * with U unit upper triangular (stored above the diagonal, D on it). */
+static void ldl_factor(int n, double* A) {
+  for (int j = 0; j < n; ++j) {
+    double d = A[j + j * n];
+    for (int k = 0; k < j; ++k) d -= A[k + j * n] * A[k + j * n] * A[k + k * n];
+    A[j + j * n] = d;
+    for (int i = j + 1; i < n; ++i) {
+      double s = A[j + i * n];
+      for (int k = 0; k < j; ++k) s -= A[k + j * n] * A[k + i * n] * A[k + k * n];
+      A[j + i * n] = s / d;
+    }
+  }
+}
+
+/* Solve M X = B for nrhs columns (LAPACKE_dsytrs, solver.cpp:505-506,532-533). */
+static void mass_solve(const ldgo* o, double* B, long nrhs) {
+  int n = o->n;
+  if (o->dsytrs) {
+    o->dsytrs(102, 'U', n, (int)nrhs, o->Mel, n, o->Mipiv, B, n);
+    return;
+  }
+  const double* A = o->Mel;
+  long j;
+#pragma omp parallel for schedule(static)
+  for (j = 0; j < nrhs; ++j) {
+    double* b = B + j * n;
+    for (int i = 0; i < n; ++i) { /* U^T y = b */
+      double s = b[i];
+      for (int k = 0; k < i; ++k) s -= A[k + i * n] * b[k];
+      b[i] = s;
+    }
+    for (int i = 0; i < n; ++i) b[i] /= A[i + i * n];
+    for (int i = n - 1; i >= 0; --i) { /* U x = z */
+      double s = b[i];
+      for (int k = i + 1; k < n; ++k) s -= A[i + k * n] * b[k];
+      b[i] = s;
+    }
+  }
+}
+
+/* ---------------------------------------------------------- dgMath restated */
+
+/* Chebyshev-Gauss-Lobatto points cos((p-i)pi/p) (dgMath.cpp:37-45). */
+static void chebyshev(int p, double* x) {
+  for (int i = 0; i <= p; ++i) x[i] = cos((p - i) * M_PI / p);
+}
+
+/* Cyclic Jacobi eigenvalue iteration on a small symmetric matrix (Jacobi
+ * 1846; Golub & Van Loan sec. 8.5).  A is n x n column-major, destroyed;
+ * V receives eigenvectors in columns; eigenvalues sorted ascending. */
+static void sym_eig(int n, double* A, double* V, double* lam) {
+  for (int i = 0; i < n * n; ++i) V[i] = 0.0;
+  for (int i = 0; i < n; ++i) V[i + i * n] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int q = 0; q < n; ++q)
+      for (int pp = 0; pp < q; ++pp) off += A[pp + q * n] * A[pp + q * n];
+    if (off < 1e-300) break;
+    for (int pp = 0; pp < n; ++pp)
+      for (int q = pp + 1; q < n; ++q) {
+        double apq = A[pp + q * n];
+        if (apq == 0.0) continue;
+        double app = A[pp + pp * n], aqq = A[q + q * n];
+        double theta = (aqq - app) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) { /* A <- A J */
+          double akp = A[k + pp * n], akq = A[k + q * n];
+          A[k + pp * n] = c * akp - s * akq;
+          A[k + q * n] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) { /* A <- J^T A */
+          double apk = A[pp + k * n], aqk = A[q + k * n];
+          A[pp + k * n] = c * apk - s * aqk;
+          A[q + k * n] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          double vkp = V[k + pp * n], vkq = V[k + q * n];
+          V[k + pp * n] = c * vkp - s * vkq;
+          V[k + q * n] = s * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < n; ++i) lam[i] = A[i + i * n];
+  for (int i = 0; i < n; ++i) /* selection sort ascending, carrying vectors */
+    for (int j = i + 1; j < n; ++j)
+      if (lam[j] < lam[i]) {
+        double t = lam[i]; lam[i] = lam[j]; lam[j] = t;
+        for (int k = 0; k < n; ++k) { t = V[k + i * n]; V[k + i * n] = V[k + j * n]; V[k + j * n] = t; }
+      }
+}
+
+/* Gauss-Legendre rule exact to degree p via the Golub-Welsch eigenproblem of
+ * the Jacobi matrix (dgMath.cpp:91-114): n = ceil((p+1)/2) points. */
+static int gauss_quad(int p, double* x, double* w) {
+  int n = (int)ceil((p + 1) / 2.0);
+  double* T = (double*)calloc((size_t)n * n, sizeof(double));
+  double* V = (double*)calloc((size_t)n * n, sizeof(double));
+  for (int i = 0; i < n - 1; ++i) {
+    double b = (i + 1) / sqrt(4.0 * (i + 1) * (i + 1) - 1);
+    T[i + (i + 1) * n] = b;
+    T[(i + 1) + i * n] = b;
+  }
+  sym_eig(n, T, V, x);
+  for (int i = 0; i < n; ++i) w[i] = 2 * V[0 + i * n] * V[0 + i * n];
+  free(T);
+  free(V);
+  return n;
+}
+
+/* Legendre polynomials 0..p and derivatives at nx points, (nx, p+1) column
+ * major, by the three-term recurrences of dgMath.cpp:177-248. */
+static void legendre(int p, int nx, const double* x, double* P, double* dP) {
+  for (int i = 0; i < nx; ++i) { P[i] = 1.0; if (dP) dP[i] = 0.0; }
+  if (p == 0) return;
+  for (int i = 0; i < nx; ++i) { P[i + nx] = x[i]; if (dP) dP[i + nx] = 1.0; }
+  for (int ip = 0; ip < p - 1; ++ip)
+    for (int i = 0; i < nx; ++i) {
+      P[i + (ip + 2) * nx] = ((2 * ip + 3) * x[i] * P[i + (ip + 1) * nx] - (ip + 1) * P[i + ip * nx]) / (ip + 2);
+      if (dP)
+        dP[i + (ip + 2) * nx] = ((2 * ip + 3) * (x[i] * dP[i + (ip + 1) * nx] + P[i + (ip + 1) * nx]) -
+                                 (ip + 1) * dP[i + ip * nx]) / (ip + 2);
+    }
+}
+
+/* Tensor-product Legendre basis on a tensor grid of 1-D points x (m per
+ * direction), d = 2 or 3 dimensions: out(pt, mode) with pt and mode both
+ * x-fastest (dgMath.cpp:254-294, 361-411).  deriv = -1 for values, or the
+ * differentiated direction (dgMath.cpp:300-355, 417-501). */
+static void legendre_nd(int p, int d, int m, const double* x, int deriv, double* out) {
+  int N = p + 1;
+  double* P = (double*)malloc(sizeof(double) * m * N);
+  double* dP = (double*)malloc(sizeof(double) * m * N);
+  legendre(p, m, x, P, dP);
+  int npts = d == 2 ? m * m : m * m * m;
+  int nmod = d == 2 ? N * N : N * N * N;
+  for (int md = 0; md < nmod; ++md) {
+    int mi[3] = {md % N, (md / N) % N, md / (N * N)};
+    for (int pt = 0; pt < npts; ++pt) {
+      int pi[3] = {pt % m, (pt / m) % m, pt / (m * m)};
+      double v = 1.0;
+      for (int l = 0; l < d; ++l) v *= (l == deriv ? dP : P)[pi[l] + mi[l] * m];
+      out[pt + (long)md * npts] = v;
+    }
+  }
+  free(P);
+  free(dP);
+}
+
+/* Interpolation matrix from the tensor CGL nodes to the tensor Gauss points
+ * in d dimensions: lTo * inv(lFrom) (dgMath.cpp:545-615). */
+static void interp_matrix(int p, int d, const double* xFrom, int mTo, const double* xTo, double* I) {
+  int N = p + 1;
+  int nFrom = d == 2 ? N * N : N * N * N;
+  int nTo = d == 2 ? mTo * mTo : mTo * mTo * mTo;
+  double* lFrom = (double*)malloc(sizeof(double) * nFrom * nFrom);
+  double* coeffs = (double*)calloc((size_t)nFrom * nFrom, sizeof(double));
+  double* lTo = (double*)malloc(sizeof(double) * nTo * nFrom);
+  legendre_nd(p, d, N, xFrom, -1, lFrom);
+  for (int i = 0; i < nFrom; ++i) coeffs[i + i * nFrom] = 1.0;
+  lu_solve(nFrom, lFrom, nFrom, coeffs);
+  legendre_nd(p, d, mTo, xTo, -1, lTo);
+  gemm(NULL, 0, nTo, nFrom, nFrom, 1.0, lTo, nTo, coeffs, nFrom, 0.0, I, nTo);
+  free(lFrom);
+  free(coeffs);
+  free(lTo);
+}
+
+/* Face-node map (mesh.cpp:428-501): face f of every element, point
+ * j = a + m*b over its two tangential directions in increasing order. */
+static void face_map(int m, int* ef) {
+  int nf = m * m;
+  for (int f = 0; f < NF; ++f) {
+    int l = f / 2, end = (f % 2) ? m - 1 : 0;
+    for (int b = 0; b < m; ++b)
+      for (int a = 0; a < m; ++a) {
+        int c[3];
+        c[l] = end;
+        c[l == 0 ? 1 : 0] = a;
+        c[l == 2 ? 1 : 2] = b;
+        ef[a + m * b + nf * f] = c[0] + m * c[1] + m * m * c[2];
+      }
+  }
+}
+
+/* ----------------------------------------------------------------- setup */
+
+void ldgo_destroy(ldgo* o);
+
+static int ldgo_setup(ldgo* o) {
+  int p = o->p, N = p + 1, n = N * N * N, nf = N * N, nE = o->nE;
+  o->N = N; o->n = n; o->nf = nf;
+  double cheb[16], xq[16], wq[16];
+  chebyshev(p, cheb);
+  int nq = gauss_quad(2 * p, xq, wq);
+  if (nq != N) return -2;
+  /* Interp2D, Interp3D (solver.cpp:74-92) */
+  o->Interp2D = (double*)malloc(sizeof(double) * nf * nf);
+  o->Interp3D = (double*)malloc(sizeof(double) * n * n);
+  interp_matrix(p, 2, cheb, N, xq, o->Interp2D);
+  interp_matrix(p, 3, cheb, N, xq, o->Interp3D);
+  /* precomputeLocalMatrices (solver.cpp:95-192) */
+  double* l3D = (double*)malloc(sizeof(double) * n * n);
+  double* coeffs = (double*)calloc((size_t)n * n, sizeof(double));
+  legendre_nd(p, 3, N, cheb, -1, l3D);
+  for (int i = 0; i < n; ++i) coeffs[i + i * n] = 1.0;
+  lu_solve(n, l3D, n, coeffs);
+  double* polyQ = (double*)malloc(sizeof(double) * n * n);
+  double* dpolyQ = (double*)malloc(sizeof(double) * n * n * DIM);
+  legendre_nd(p, 3, N, xq, -1, polyQ);
+  for (int l = 0; l < DIM; ++l) legendre_nd(p, 3, N, xq, l, dpolyQ + (long)l * n * n);
+  double* phiQ = (double*)malloc(sizeof(double) * n * n);
+  double* dphiQ = (double*)malloc(sizeof(double) * n * n * DIM);
+  gemm(NULL, 0, n, n, n, 1.0, polyQ, n, coeffs, n, 0.0, phiQ, n);
+  for (int l = 0; l < DIM; ++l)
+    gemm(NULL, 0, n, n, n, 1.0, dpolyQ + (long)l * n * n, n, coeffs, n, 0.0, dphiQ + (long)l * n * n, n);
+  o->wQ3 = (double*)malloc(sizeof(double) * n);
+  for (int iz = 0; iz < N; ++iz)
+    for (int iy = 0; iy < N; ++iy)
+      for (int ix = 0; ix < N; ++ix) o->wQ3[ix + N * iy + N * N * iz] = wq[ix] * wq[iy] * wq[iz];
+  for (int j = 0; j < n; ++j)
+    for (int q = 0; q < n; ++q) polyQ[q + j * n] = phiQ[q + j * n] * o->wQ3[q];
+  o->alpha[0] = o->minDX / 2.0;
+  o->alpha[1] = o->minDY / 2.0;
+  o->alpha[2] = o->minDZ / 2.0;
+  o->J = o->alpha[0] * o->alpha[1] * o->alpha[2];
+  o->Mel = (double*)malloc(sizeof(double) * n * n);
+  o->Mipiv = (int*)calloc(n, sizeof(int));
+  gemm(NULL, 1, n, n, n, o->J, polyQ, n, phiQ, n, 0.0, o->Mel, n);
+  if (o->dsytrf)
+    o->dsytrf(102, 'U', n, o->Mel, n, o->Mipiv);
+  else
+    ldl_factor(n, o->Mel);
+  o->Sels = (double*)malloc(sizeof(double) * n * n * DIM);
+  o->Kels = (double*)malloc(sizeof(double) * n * n * DIM);
+  o->Kels2D = (double*)malloc(sizeof(double) * nf * nf * DIM);
+  double w2[64];
+  for (int b = 0; b < N; ++b)
+    for (int a = 0; a < N; ++a) w2[a + N * b] = wq[a] * wq[b];
+  for (int l = 0; l < DIM; ++l) {
+    double scaleL = o->J / o->alpha[l];
+    gemm(NULL, 1, n, n, n, scaleL, dphiQ + (long)l * n * n, n, polyQ, n, 0.0, o->Sels + (long)l * n * n, n);
+    for (int i = 0; i < n; ++i)
+      for (int q = 0; q < n; ++q)
+        o->Kels[q + (long)i * n + (long)l * n * n] = dphiQ[q + (long)i * n + (long)l * n * n] * o->wQ3[q] * scaleL;
+    for (int i = 0; i < nf; ++i)
+      for (int q = 0; q < nf; ++q)
+        o->Kels2D[q + i * nf + l * nf * nf] = o->Interp2D[q + i * nf] * w2[q] * scaleL;
+  }
+  free(l3D); free(coeffs); free(polyQ); free(dpolyQ); free(phiQ); free(dphiQ);
+  /* Mesh connectivity (mesh.cpp:201-353): periodic neighbours directly. */
+  o->efToN = (int*)malloc(sizeof(int) * nf * NF);
+  face_map(N, o->efToN);
+  o->eToE = (int*)malloc(sizeof(int) * NF * nE);
+  for (int iz = 0; iz < o->nz; ++iz)
+    for (int iy = 0; iy < o->ny; ++iy)
+      for (int ix = 0; ix < o->nx; ++ix) {
+        int e = ix + o->nx * (iy + o->ny * iz);
+        int c[3] = {ix, iy, iz}, dims[3] = {o->nx, o->ny, o->nz};
+        for (int f = 0; f < NF; ++f) {
+          int cc[3] = {c[0], c[1], c[2]};
+          int l = f / 2;
+          cc[l] = (c[l] + ((f % 2) ? 1 : dims[l] - 1)) % dims[l];
+          o->eToE[f + NF * e] = cc[0] + o->nx * (cc[1] + o->ny * cc[2]);
+        }
+      }
+  long nU = (long)n * NS * nE;
+  o->uCurr = (double*)calloc(nU, sizeof(double));
+  o->uInterp2D = (double*)calloc((long)nf * NS * NF * nE, sizeof(double));
+  o->uInterp3D = (double*)calloc(nU, sizeof(double));
+  o->ks = (double*)calloc(nU * 4, sizeof(double));
+  o->Dus = (double*)calloc(nU * DIM, sizeof(double));
+  o->DuInterp2D = (double*)calloc((long)nf * NS * NF * nE * DIM, sizeof(double));
+  o->DuInterp3D = (double*)calloc(nU * DIM, sizeof(double));
+  o->onFaces = (double*)calloc((long)nf * NS * NF * nE * DIM, sizeof(double));
+  o->flx = (double*)calloc(nU * DIM, sizeof(double));
+  if (!o->uCurr || !o->ks || !o->Dus || !o->DuInterp2D || !o->DuInterp3D || !o->onFaces || !o->flx)
+    return -3;
+  return 0;
+}
+
+/* Solver constructor essentials (solver.cpp:7-71): physics, CFL dt rule. */
+ldgo* ldgo_create(int nx, int ny, int nz, int p, double L, double tf, double Re, int threads) {
+  if (nx < 3 || ny < 3 || nz < 3 || p < 1 || p > 7) return NULL; /* mesh.cpp:102-107 */
+  ldgo* o = (ldgo*)calloc(1, sizeof(ldgo));
+  o->p = p; o->nx = nx; o->ny = ny; o->nz = nz; o->nE = nx * ny * nz; o->L = L;
+  o->threads = threads > 0 ? threads : 1;
+#ifdef _OPENMP
+  omp_set_num_threads(o->threads);
+#endif
+  o->Re = Re; o->Pr = .71; o->gamma = 1.4; o->M0 = 0.1; o->R = 8.314; o->rho0 = 1.0; o->V0 = 1.0;
+  o->c0 = o->V0 / o->M0;
+  o->p0 = o->rho0 * o->c0 * o->c0 / o->gamma;
+  o->T0 = o->p0 / (o->R * o->rho0);
+  double size = M_PI * L;
+  o->minDX = (size - (-size)) / nx;
+  o->minDY = (size - (-size)) / ny;
+  o->minDZ = (size - (-size)) / nz;
+  double maxVel = o->V0;
+  double m = o->minDX < o->minDY ? o->minDX : o->minDY;
+  m = m < o->minDZ ? m : o->minDZ;
+  o->dt = 0.01 * m / (maxVel * (2 * p + 1));
+  o->timesteps = (long)ceil(tf / o->dt);
+  if (o->timesteps < 1) o->timesteps = 1;
+  o->dt = tf / o->timesteps;
+  if (ldgo_setup(o) != 0) { ldgo_destroy(o); return NULL; }
+  return o;
+}
+
+/* Route GEMM and the mass solve to an OpenBLAS library (scipy's bundled
+ * build exports scipy_-prefixed names).  Must be called before ldgo_create
+ * of the solvers that should use it; returns 0 on success. */
+static void* g_blas = NULL;
+static dgemm_fn g_dgemm = NULL;
+static dsytrf_fn g_dsytrf = NULL;
+static dsytrs_fn g_dsytrs = NULL;
+int ldgo_use_openblas(const char* path, int threads) {
+  if (!path) { g_dgemm = NULL; g_dsytrf = NULL; g_dsytrs = NULL; return 0; }
+  void* h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+  if (!h) return -1;
+  const char* pre[2] = {"scipy_", ""};
+  for (int i = 0; i < 2; ++i) {
+    char b1[64], b2[64], b3[64], b4[64];
+    snprintf(b1, 64, "%scblas_dgemm", pre[i]);
+    snprintf(b2, 64, "%sLAPACKE_dsytrf", pre[i]);
+    snprintf(b3, 64, "%sLAPACKE_dsytrs", pre[i]);
+    snprintf(b4, 64, "%sopenblas_set_num_threads", pre[i]);
+    dgemm_fn g = (dgemm_fn)dlsym(h, b1);
+    dsytrf_fn f = (dsytrf_fn)dlsym(h, b2);
+    dsytrs_fn s = (dsytrs_fn)dlsym(h, b3);
+    setthreads_fn t = (setthreads_fn)dlsym(h, b4);
+    if (g && f && s) {
+      if (t) t(threads > 0 ? threads : 1);
+      g_blas = h; g_dgemm = g; g_dsytrf = f; g_dsytrs = s;
+      return 0;
+    }
+  }
+  dlclose(h);
+  return -2;
+}
+
+ldgo* ldgo_create_blas(int nx, int ny, int nz, int p, double L, double tf, double Re, int threads) {
+  /* Same as ldgo_create but picks up the OpenBLAS routes (if loaded) before
+   * the mass matrix is factored. */
+  if (nx < 3 || ny < 3 || nz < 3 || p < 1 || p > 7) return NULL;
+  ldgo* o = (ldgo*)calloc(1, sizeof(ldgo));
+  o->p = p; o->nx = nx; o->ny = ny; o->nz = nz; o->nE = nx * ny * nz; o->L = L;
+  o->threads = threads > 0 ? threads : 1;
+#ifdef _OPENMP
+  omp_set_num_threads(o->threads);
+#endif
+  o->dgemm = g_dgemm; o->dsytrf = g_dsytrf; o->dsytrs = g_dsytrs;
+  o->Re = Re; o->Pr = .71; o->gamma = 1.4; o->M0 = 0.1; o->R = 8.314; o->rho0 = 1.0; o->V0 = 1.0;
+  o->c0 = o->V0 / o->M0;
+  o->p0 = o->rho0 * o->c0 * o->c0 / o->gamma;
+  o->T0 = o->p0 / (o->R * o->rho0);
+  double size = M_PI * L;
+  o->minDX = (size - (-size)) / nx;
+  o->minDY = (size - (-size)) / ny;
+  o->minDZ = (size - (-size)) / nz;
+  double m = o->minDX < o->minDY ? o->minDX : o->minDY;
+  m = m < o->minDZ ? m : o->minDZ;
+  o->dt = 0.01 * m / (o->V0 * (2 * p + 1));
+  o->timesteps = (long)ceil(tf / o->dt);
+  if (o->timesteps < 1) o->timesteps = 1;
+  o->dt = tf / o->timesteps;
+  if (ldgo_setup(o) != 0) { ldgo_destroy(o); return NULL; }
+  return o;
+}
+
+void ldgo_destroy(ldgo* o) {
+  if (!o) return;
+  free(o->Interp2D); free(o->Interp3D); free(o->Mel); free(o->Mipiv); free(o->Sels);
+  free(o->Kels); free(o->Kels2D); free(o->wQ3); free(o->efToN); free(o->eToE);
+  free(o->uCurr); free(o->uInterp2D); free(o->uInterp3D); free(o->ks); free(o->Dus);
+  free(o->DuInterp2D); free(o->DuInterp3D); free(o->onFaces); free(o->flx);
+  free(o);
+}
+
+double ldgo_dt(const ldgo* o) { return o->dt; }
+long ldgo_timesteps(const ldgo* o) { return o->timesteps; }
+int ldgo_dofs(const ldgo* o) { return o->n; }
+int ldgo_nelements(const ldgo* o) { return o->nE; }
+void ldgo_set_dt(ldgo* o, double dt) { o->dt = dt; }
+
+/* Copies the reference operators out for white-box tests:
+ * which 0 Interp2D (nf*nf), 1 Interp3D (n*n), 2 Kels (n*n*3), 3 Kels2D
+ * (nf*nf*3), 4 Sels (n*n*3), 5 wQ3 (n). */
+int ldgo_get_operator(const ldgo* o, int which, double* out) {
+  long n = o->n, nf = o->nf;
+  switch (which) {
+    case 0: memcpy(out, o->Interp2D, sizeof(double) * nf * nf); return 0;
+    case 1: memcpy(out, o->Interp3D, sizeof(double) * n * n); return 0;
+    case 2: memcpy(out, o->Kels, sizeof(double) * n * n * 3); return 0;
+    case 3: memcpy(out, o->Kels2D, sizeof(double) * nf * nf * 3); return 0;
+    case 4: memcpy(out, o->Sels, sizeof(double) * n * n * 3); return 0;
+    case 5: memcpy(out, o->wQ3, sizeof(double) * n); return 0;
+  }
+  return -1;
+}
+
+/* Taylor-Green initial condition at the element nodes (solver.cpp:194-236,
+ * node coordinates mesh.cpp:127-151,389-408). */
+void ldgo_initial_condition(const ldgo* o, double* u) {
+  int N = o->N, n = o->n, p = o->p;
+  double cheb[16];
+  chebyshev(p, cheb);
+  double size = M_PI * o->L;
+  double bl = -size, tr = size;
+  for (int iz = 0; iz < o->nz; ++iz)
+    for (int iy = 0; iy < o->ny; ++iy)
+      for (int ix = 0; ix < o->nx; ++ix) {
+        int k = ix + o->nx * (iy + o->ny * iz);
+        double x0 = ix * (tr - bl) / o->nx + bl, x1 = (ix + 1) * (tr - bl) / o->nx + bl;
+        double y0 = iy * (tr - bl) / o->ny + bl, y1 = (iy + 1) * (tr - bl) / o->ny + bl;
+        double z0 = iz * (tr - bl) / o->nz + bl, z1 = (iz + 1) * (tr - bl) / o->nz + bl;
+        for (int c = 0; c < N; ++c)
+          for (int b = 0; b < N; ++b)
+            for (int a = 0; a < N; ++a) {
+              int v = a + N * b + N * N * c;
+              double x = x0 + .5 * (cheb[a] + 1.0) * (x1 - x0);
+              double y = y0 + .5 * (cheb[b] + 1.0) * (y1 - y0);
+              double z = z0 + .5 * (cheb[c] + 1.0) * (z1 - z0);
+              double L = o->L;
+              double pr = o->p0 + (o->rho0 * o->V0 * o->V0 / 16.0) * (cos(2 * x / L) + cos(2 * y / L)) *
+                                      (cos(2 * z / L) + 2);
+              double* uk = u + (long)k * n * NS;
+              uk[v + 0 * n] = pr / (o->R * o->T0);
+              uk[v + 1 * n] = o->rho0 * o->V0 * sin(x / L) * cos(y / L) * cos(z / L);
+              uk[v + 2 * n] = -o->rho0 * o->V0 * cos(x / L) * sin(y / L) * cos(z / L);
+              uk[v + 3 * n] = 0 * o->rho0;
+              uk[v + 4 * n] = pr / (o->gamma - 1) + (uk[v + 1 * n] * uk[v + 1 * n] + uk[v + 2 * n] * uk[v + 2 * n] +
+                                                     uk[v + 3 * n] * uk[v + 3 * n]) / (2.0 * uk[v + 0 * n]);
+            }
+      }
+}
+
+/* --------------------------------------------------------- pointwise fluxes */
+
+/* Euler flux, fluxes[iS + 5*l] (solver.cpp:1040-1086). */
+static void flux_c(const ldgo* o, const double* u, double* f) {
+  double ir = 1.0 / u[0];
+  double mx = u[1], my = u[2], mz = u[3], E = u[4];
+  double pr4 = 0.2e1 / 0.5e1 * E;                   /* (gamma-1) E */
+  double ke4 = (mx * mx + my * my + mz * mz) * ir / 0.5e1; /* (gamma-1)|m|^2/(2 rho) */
+  double H = o->gamma * E - ke4;
+  f[0] = mx; f[1] = mx * mx * ir + pr4 - ke4; f[2] = mx * my * ir; f[3] = mx * mz * ir; f[4] = mx * H * ir;
+  f[5] = my; f[6] = f[2]; f[7] = my * my * ir + pr4 - ke4; f[8] = my * mz * ir; f[9] = my * H * ir;
+  f[10] = mz; f[11] = f[3]; f[12] = f[8]; f[13] = mz * mz * ir + pr4 - ke4; f[14] = mz * H * ir;
+}
+
+/* Navier-Stokes viscous flux from u and its gradient Du[iS + 5*l]
+ * (solver.cpp:1089-1188): Newtonian stress with Stokes' hypothesis scaled
+ * by 1/Re, heat flux gamma/Pr * grad(e)/Re. */
+static void flux_v(const ldgo* o, const double* u, const double* Du, double* f) {
+  double ir = 1.0 / u[0];
+  double v[3] = {u[1] * ir, u[2] * ir, u[3] * ir};
+  double G[3][3]; /* G[i][j] = d_j v_i */
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) G[i][j] = (Du[(1 + i) + 5 * j] - Du[0 + 5 * j] * v[i]) * ir;
+  double div = G[0][0] + G[1][1] + G[2][2];
+  double iRe = 1.0 / o->Re, kap = o->gamma / o->Pr;
+  double tau[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) tau[i][j] = (G[i][j] + G[j][i] - (i == j ? 2.0 / 3.0 * div : 0.0));
+  double e = u[4] * ir;
+  for (int j = 0; j < 3; ++j) {
+    double de = (Du[4 + 5 * j] - Du[0 + 5 * j] * e) * ir - (v[0] * G[0][j] + v[1] * G[1][j] + v[2] * G[2][j]);
+    f[0 + 5 * j] = 0.0;
+    for (int i = 0; i < 3; ++i) f[1 + i + 5 * j] = tau[i][j] * iRe;
+    f[4 + 5 * j] = (tau[0][j] * v[0] + tau[1][j] * v[1] + tau[2][j] * v[2] + kap * de) * iRe;
+  }
+}
+
+/* Roe flux F(uN, uK, n) from element K's side (solver.cpp:1194-1374),
+ * gamma = 1.4 hard-coded as in the reference. */
+static void flux_roe(const double* uN, const double* uK, const double* nrm, double* f) {
+  const double g1 = 0.4;
+  double rN = uN[0], rK = uK[0], irN = 1.0 / rN, irK = 1.0 / rK;
+  double vN[3] = {uN[1] * irN, uN[2] * irN, uN[3] * irN};
+  double vK[3] = {uK[1] * irK, uK[2] * irK, uK[3] * irK};
+  double qN = vN[0] * nrm[0] + vN[1] * nrm[1] + vN[2] * nrm[2];
+  double qK = vK[0] * nrm[0] + vK[1] * nrm[1] + vK[2] * nrm[2];
+  double pN = g1 * uN[4] - 0.5 * g1 * rN * (vN[0] * vN[0] + vN[1] * vN[1] + vN[2] * vN[2]);
+  double pK = g1 * uK[4] - 0.5 * g1 * rK * (vK[0] * vK[0] + vK[1] * vK[1] + vK[2] * vK[2]);
+  double s = sqrt(rN * irK); /* sqrt(rhoN/rhoK) */
+  double is1 = 1.0 / (s + 1.0);
+  double vt[3];
+  for (int i = 0; i < 3; ++i) vt[i] = (s * vN[i] + vK[i]) * is1;
+  double Ht = (s * (uN[4] + pN) * irN + (uK[4] + pK) * irK) * is1;
+  double vt2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
+  double qt = vt[0] * nrm[0] + vt[1] * nrm[1] + vt[2] * nrm[2];
+  double c2 = g1 * (Ht - 0.5 * vt2), c = sqrt(c2);
+  double l0 = fabs(qt), lp = 0.5 * fabs(qt + c), lm = 0.5 * fabs(-qt + c);
+  double dr = rN - rK, dm[3] = {uN[1] - uK[1], uN[2] - uK[2], uN[3] - uK[3]}, dE = uN[4] - uK[4];
+  double a1 = lp + lm - l0;
+  double dp = g1 * (0.5 * vt2 * dr - (vt[0] * dm[0] + vt[1] * dm[1] + vt[2] * dm[2]) + dE);
+  double dq = -qt * dr + dm[0] * nrm[0] + dm[1] * nrm[1] + dm[2] * nrm[2];
+  double a2 = lp - lm;
+  double t158 = a1 * dp / c2, t168 = a2 * dq / c;
+  double t179 = t158 + t168, t186 = a2 * dp / c + a1 * dq;
+  f[0] = 0.5 * rN * qN + 0.5 * rK * qK - 0.5 * l0 * dr - 0.5 * t179;
+  for (int i = 0; i < 3; ++i)
+    f[1 + i] = 0.5 * uN[1 + i] * qN + 0.5 * uK[1 + i] * qK + 0.5 * nrm[i] * (pN + pK) - 0.5 * l0 * dm[i] -
+               0.5 * t179 * vt[i] - 0.5 * t186 * nrm[i];
+  f[4] = 0.5 * (uN[4] + pN) * qN + 0.5 * (uK[4] + pK) * qK - 0.5 * l0 * dE - 0.5 * t179 * Ht - 0.5 * t186 * qt;
+}
+
+/* ------------------------------------------------------------------ RHS */
+
+/* Gather face nodes and interpolate to face/volume quadrature points
+ * (solver.cpp:541-577); periodic neighbours replace the ghost exchange
+ * (solver.cpp:929-998). dim = 1 (u) or 3 (Du). */
+static void interpolate(ldgo* o, const double* curr, double* i2d, double* i3d, int dim) {
+  int n = o->n, nf = o->nf, nE = o->nE;
+  long blk = (long)nf * NS * NF * nE;
+  for (int l = 0; l < dim; ++l) {
+    long k;
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < nE; ++k)
+      for (int f = 0; f < NF; ++f)
+        for (int s = 0; s < NS; ++s)
+          for (int j = 0; j < nf; ++j)
+            o->onFaces[j + nf * (s + NS * (f + NF * k)) + l * blk] =
+                curr[o->efToN[j + nf * f] + n * (s + NS * k) + (long)l * n * NS * nE];
+    gemm(o, 0, nf, NS * NF * nE, nf, 1.0, o->Interp2D, nf, o->onFaces + l * blk, nf, 0.0, i2d + l * blk, nf);
+  }
+  gemm(o, 0, n, NS * nE * dim, n, 1.0, o->Interp3D, n, curr, n, 0.0, i3d, n);
+}
+
+/* Adds Kels2D(:,:,f/2)^T * fstar into the face nodes of res (the per-face
+ * DGEMM + scatter of solver.cpp:618-629). */
+static void face_lift(const ldgo* o, int f, const double* fstar, double* res) {
+  int n = o->n, nf = o->nf;
+  const double* K2 = o->Kels2D + (long)(f / 2) * nf * nf;
+  for (int s = 0; s < NS; ++s)
+    for (int j = 0; j < nf; ++j) {
+      double acc = 0.0;
+      for (int q = 0; q < nf; ++q) acc += K2[q + j * nf] * fstar[q + nf * s];
+      res[o->efToN[j + nf * f] + n * s] += acc;
+    }
+}
+
+static const double kNormals[NF][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+
+/* One RHS evaluation k = rhs(uCurr) (rk4Rhs, solver.cpp:486-535). */
+void ldgo_rhs(ldgo* o, const double* uCurr, double* k) {
+  int n = o->n, nf = o->nf, nE = o->nE;
+  long nU = (long)n * NS * nE;
+  long fblk = (long)nf * NS * NF * nE;
+  interpolate(o, uCurr, o->uInterp2D, o->uInterp3D, 1);
+  /* Gradient pass: Dus_l = Mel \ (-S_l u + F_l(u))  (solver.cpp:495-508) */
+  memset(o->Dus, 0, sizeof(double) * nU * DIM);
+  long e;
+#pragma omp parallel for schedule(static)
+  for (e = 0; e < nE; ++e) { /* localDGFlux (solver.cpp:585-635) */
+    double fstar[NS * 64];
+    for (int l = 0; l < DIM; ++l)
+      for (int f = 0; f < NF; ++f) {
+        int nK = o->eToE[f + NF * e], nF = f ^ 1;
+        double nl = kNormals[f][l];
+        for (int s = 0; s < NS; ++s)
+          for (int q = 0; q < nf; ++q) {
+            double uK = o->uInterp2D[q + nf * (s + NS * (f + NF * e))];
+            double uN = o->uInterp2D[q + nf * (s + NS * (nF + NF * (long)nK))];
+            fstar[q + nf * s] = ((nl > 0) ? uK : uN) * nl; /* numericalFluxL, solver.cpp:867-884 */
+          }
+        face_lift(o, f, fstar, o->Dus + l * nU + (long)e * n * NS);
+      }
+  }
+  for (int l = 0; l < DIM; ++l) {
+    gemm(o, 0, n, NS * nE, n, -1.0, o->Sels + (long)l * n * n, n, uCurr, n, 1.0, o->Dus + l * nU, n);
+    mass_solve(o, o->Dus + l * nU, (long)NS * nE);
+  }
+  interpolate(o, o->Dus, o->DuInterp2D, o->DuInterp3D, DIM);
+  /* Residual: faces, negate, volumes, mass solve (solver.cpp:516-533) */
+  memset(k, 0, sizeof(double) * nU);
+#pragma omp parallel for schedule(static)
+  for (e = 0; e < nE; ++e) {
+    double fstar[NS * 64];
+    double uK[NS], uN[NS], DuK[NS * DIM], DuN[NS * DIM], fl[NS], Fv[NS * DIM];
+    for (int f = 0; f < NF; ++f) { /* convectDGFlux (solver.cpp:643-698) */
+      int nK = o->eToE[f + NF * e], nF = f ^ 1;
+      for (int q = 0; q < nf; ++q) {
+        for (int s = 0; s < NS; ++s) {
+          uK[s] = o->uInterp2D[q + nf * (s + NS * (f + NF * e))];
+          uN[s] = o->uInterp2D[q + nf * (s + NS * (nF + NF * (long)nK))];
+        }
+        flux_roe(uN, uK, kNormals[f], fl);
+        for (int s = 0; s < NS; ++s) fstar[q + nf * s] = fl[s];
+      }
+      face_lift(o, f, fstar, k + (long)e * n * NS);
+    }
+    for (int f = 0; f < NF; ++f) { /* viscousDGFlux (solver.cpp:750-814) */
+      int nK = o->eToE[f + NF * e], nF = f ^ 1;
+      const double* nrm = kNormals[f];
+      int kWins = (nrm[0] + nrm[1] + nrm[2]) > 0; /* numericalFluxV, solver.cpp:891-921 */
+      for (int q = 0; q < nf; ++q) {
+        for (int s = 0; s < NS; ++s) {
+          uK[s] = o->uInterp2D[q + nf * (s + NS * (f + NF * e))];
+          uN[s] = o->uInterp2D[q + nf * (s + NS * (nF + NF * (long)nK))];
+        }
+        for (int l = 0; l < DIM; ++l)
+          for (int s = 0; s < NS; ++s) {
+            DuK[s + NS * l] = o->DuInterp2D[q + nf * (s + NS * (f + NF * e)) + l * fblk];
+            DuN[s + NS * l] = o->DuInterp2D[q + nf * (s + NS * (nF + NF * (long)nK)) + l * fblk];
+          }
+        flux_v(o, uK, kWins ? DuN : DuK, Fv);
+        for (int s = 0; s < NS; ++s) {
+          double acc = 0.0;
+          for (int l = 0; l < DIM; ++l) acc -= Fv[s + NS * l] * nrm[l];
+          fstar[q + nf * s] = acc;
+        }
+      }
+      face_lift(o, f, fstar, k + (long)e * n * NS);
+    }
+    for (long i = 0; i < (long)n * NS; ++i) k[(long)e * n * NS + i] = -k[(long)e * n * NS + i]; /* dscal -1 */
+    /* Volume fluxes at quadrature points (solver.cpp:701-741, 817-864),
+     * stored as (fc - fv) per direction in flx(n,5,nE,3). */
+    for (int q = 0; q < n; ++q) {
+      double u[NS], Du[NS * DIM], Fc[NS * DIM];
+      for (int s = 0; s < NS; ++s) u[s] = o->uInterp3D[q + n * (s + NS * e)];
+      for (int l = 0; l < DIM; ++l)
+        for (int s = 0; s < NS; ++s) Du[s + NS * l] = o->DuInterp3D[q + n * (s + NS * e) + l * nU];
+      flux_c(o, u, Fc);
+      flux_v(o, u, Du, Fv);
+      for (int l = 0; l < DIM; ++l)
+        for (int s = 0; s < NS; ++s) o->flx[q + n * (s + NS * e) + l * nU] = Fc[s + NS * l] - Fv[s + NS * l];
+    }
+  }
+  for (int l = 0; l < DIM; ++l)
+    gemm(o, 1, n, NS * nE, n, 1.0, o->Kels + (long)l * n * n, n, o->flx + l * nU, n, 1.0, k, n);
+  mass_solve(o, k, (long)NS * nE);
+}
+
+/* Kinetic energy exactly as computeKE (solver.cpp:1007-1034): nodal values
+ * weighted by the Gauss weights (the reference quirk; nQ3D == dofs). */
+double ldgo_compute_ke(const ldgo* o, const double* u) {
+  int n = o->n, nE = o->nE;
+  double total = 0.0;
+  for (int e = 0; e < nE; ++e) {
+    double ke = 0.0;
+    const double* uk = u + (long)e * n * NS;
+    for (int q = 0; q < n; ++q)
+      ke += o->J * o->wQ3[q] *
+            (uk[q + n] * uk[q + n] + uk[q + 2 * n] * uk[q + 2 * n] + uk[q + 3 * n] * uk[q + 3 * n]) / (2 * uk[q]);
+    total += ke;
+  }
+  return total / (o->rho0 * pow(2 * M_PI * o->L, 3.0));
+}
+
+/* nsteps classical RK4 steps in place (solver.cpp:298-315, 410-440);
+ * ke[i] (if given) receives computeKE after step i. */
+void ldgo_step(ldgo* o, double* u, int nsteps, double* ke) {
+  const double b[4] = {1 / 6.0, 1 / 3.0, 1 / 3.0, 1 / 6.0};
+  const double a[3] = {0.5, 0.5, 1.0};
+  long nU = (long)o->n * NS * o->nE;
+  for (int it = 0; it < nsteps; ++it) {
+    for (int s = 0; s < 4; ++s) {
+      long i;
+      if (s == 0) {
+        memcpy(o->uCurr, u, sizeof(double) * nU);
+      } else {
+        const double* kp = o->ks + (long)(s - 1) * nU;
+#pragma omp parallel for schedule(static)
+        for (i = 0; i < nU; ++i) o->uCurr[i] = u[i] + o->dt * a[s - 1] * kp[i];
+      }
+      ldgo_rhs(o, o->uCurr, o->ks + (long)s * nU);
+    }
+    for (int s = 0; s < 4; ++s) {
+      const double* kp = o->ks + (long)s * nU;
+      long i;
+#pragma omp parallel for schedule(static)
+      for (i = 0; i < nU; ++i) u[i] += o->dt * b[s] * kp[i];
+    }
+    if (ke) ke[it] = ldgo_compute_ke(o, u);
+  }
+}

@@ -1,0 +1,128 @@
+"""CPU tests of the oracle (oracle/ldg_oracle.c) against the golden vectors
+produced by the unmodified reference (tests/golden/make_golden.py), plus
+known-answer checks of the discretisation it restates."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, rel_l2
+
+TOL = 1e-12  # relative L2, the FP64 parity bar
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def test_tgv_initial_condition_bitwise():
+    z = load("tgv_n8_p2.npz")
+    o = oracle.Oracle(8, 2, steps=100)
+    assert o.dt == float(z["dt"])
+    u0 = o.initial_condition()
+    assert np.array_equal(u0, z["u0"])
+
+
+def test_tgv_100_steps_matches_reference():
+    """Configuration: 8^3 p=2 Taylor-Green, 100 RK4 steps, per-step KE."""
+    z = load("tgv_n8_p2.npz")
+    o = oracle.Oracle(8, 2, steps=100, threads=4)
+    u = z["u0"].copy()
+    u, ke = o.step(u, 1)
+    assert rel_l2(u, z["u1"]) <= TOL
+    u, ke2 = o.step(u, 9)
+    assert rel_l2(u, z["u10"]) <= TOL
+    u, ke3 = o.step(u, 90)
+    assert rel_l2(u, z["u100"]) <= TOL
+    kes = np.concatenate([ke, ke2, ke3])
+    assert np.max(np.abs(kes - z["ke"]) / z["ke"]) <= 1e-13
+
+
+@pytest.mark.parametrize("name", ["rhs_n3_p1", "rhs_n3_p2", "rhs_n4_p3", "rhs_n3_p4", "rhs_n4_p2"])
+def test_rhs_matches_reference(name):
+    z = load(name + ".npz")
+    nx = int(name.split("_")[1][1:])
+    p = int(name.split("_")[2][1:])
+    o = oracle.Oracle(nx, p)
+    k = o.rhs(z["u0"])
+    assert rel_l2(k, z["k"]) <= TOL
+
+
+@pytest.mark.parametrize("name", ["step_n4_p2", "step_n3_p4", "step_n4_p3"])
+def test_steps_match_reference(name):
+    z = load(name + ".npz")
+    nx = int(name.split("_")[1][1:])
+    p = int(name.split("_")[2][1:])
+    o = oracle.Oracle(nx, p, steps=int(z["steps"]))
+    assert o.dt == float(z["dt"])
+    u, ke = o.step(z["u0"], int(z["steps"]))
+    assert rel_l2(u, z["u_final"]) <= TOL
+    assert np.max(np.abs(ke - z["ke"]) / np.abs(z["ke"])) <= 1e-13
+
+
+def test_openblas_route_matches_loops():
+    lib = oracle.find_openblas()
+    if lib is None:
+        pytest.skip("scipy's OpenBLAS not available")
+    z = load("rhs_n4_p3.npz")
+    a = oracle.Oracle(4, 3).rhs(z["u0"])
+    b = oracle.Oracle(4, 3, openblas=lib, threads=2).rhs(z["u0"])
+    assert rel_l2(b, a) <= 1e-13
+
+
+# ---------------------------------------------------------- known answers
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5])
+def test_gauss_rule_is_gauss_legendre(p):
+    o = oracle.Oracle(3, p)
+    w3 = o.operator(5)
+    x, w = np.polynomial.legendre.leggauss(p + 1)
+    ref = np.einsum("i,j,k->kji", w, w, w).ravel()
+    assert np.allclose(w3, ref, rtol=1e-14, atol=1e-15)
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_interp3d_exact_on_polynomials(p):
+    """Interp3D maps nodal values of a degree<=p polynomial to its values at
+    the Gauss points (dgMath.cpp:583-615)."""
+    o = oracle.Oracle(3, p)
+    n = (p + 1) ** 3
+    I3 = o.operator(1).reshape(n, n, order="F")
+    xi = np.cos((p - np.arange(p + 1)) * np.pi / p)
+    xq, _ = np.polynomial.legendre.leggauss(p + 1)
+    f = lambda x, y, z: 1 + 2 * x ** p - y * z ** (p - 1) + 0.5 * x * y * z
+    X, Y, Z = np.meshgrid(xi, xi, xi, indexing="ij")
+    nodal = f(X, Y, Z).transpose(2, 1, 0).ravel()  # x fastest
+    Xq, Yq, Zq = np.meshgrid(xq, xq, xq, indexing="ij")
+    exact = f(Xq, Yq, Zq).transpose(2, 1, 0).ravel()
+    assert np.allclose(I3 @ nodal, exact, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_free_stream_preserved(p):
+    """A constant state is a steady solution: the RHS vanishes."""
+    o = oracle.Oracle(3, p)
+    u = np.zeros(o.shape)
+    u[:, 0], u[:, 1], u[:, 2], u[:, 3], u[:, 4] = 1.2, 0.3, -0.2, 0.1, 180.0
+    k = o.rhs(u)
+    assert np.max(np.abs(k)) <= 1e-10
+
+
+def test_tgv_initial_kinetic_energy():
+    o = oracle.Oracle(8, 2)
+    ke = o.ke(o.initial_condition())
+    assert abs(ke - 0.125) < 1e-3
+
+
+def test_conservation_of_mass():
+    """Periodic DG with the (antisymmetric) Roe flux conserves total mass.
+    Momentum and energy are not conserved exactly by the reference scheme:
+    its viscous face flux evaluates each side with its own trace of u
+    (numericalFluxV, solver.cpp:897-912), so the two sides' fluxes differ."""
+    z = load("step_n4_p2.npz")
+    o = oracle.Oracle(4, 2, steps=5)
+    n = o.dofs
+    c = o.operator(1).reshape(n, n, order="F").T @ o.operator(5)  # integrals of the nodal basis
+    tot = lambda u: np.einsum("evq,q->v", u, c)
+    u, _ = o.step(z["u0"], 5)
+    assert abs(tot(u)[0] - tot(z["u0"])[0]) <= 1e-13 * abs(tot(z["u0"])[0])
