@@ -163,6 +163,31 @@ int ldg_kernel_times(ldg_solver* s, double* ms, long long* launches, int max_cla
  * kernels.  (No reference counterpart.) */
 int ldg_probe_fp64_peak(int device, double* tflops);
 
+/* RHS evaluation without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot let the library allocate
+ * device memory -- an application whose memory is owned by its own arena or
+ * by another framework's caching allocator, or a real-time loop in which a
+ * cudaMalloc (which may synchronise the device and can fail under
+ * fragmentation) is not allowed.  Such callers cannot use ldg_create, which
+ * allocates the solver's buffers.
+ *
+ * Computes k = rhs(u) like ldg_rhs for the mesh and physics in cfg, with u
+ * and k DEVICE pointers in the reference layout (dofs, 5, nElements) on
+ * device cfg->device; work is enqueued on `stream` (a cudaStream_t; NULL =
+ * the legacy default stream) and the call returns without synchronising.
+ * Intermediate buffers live in one fixed file-scope device array of
+ * LDG_NOALLOC_SCRATCH_BYTES (64 MiB), which every GPU that loads the
+ * library holds until the process exits.  A mesh whose buffers need more
+ * (nElements * (20 (p+1)^3 + 75 (p+1)^2) * 8 bytes, i.e. about 1900
+ * elements at p=4, 3400 at p=3, 6900 at p=2) is rejected with LDG_ERR_INVALID.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls share the array and it keeps the
+ * last call's contents (every part is overwritten before it is read), so
+ * calls whose GPU work overlaps race: order them on one stream. */
+#define LDG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int ldg_rhs_noalloc(const ldg_config* cfg, const double* u_dev, double* k_dev, void* stream);
+
 const char* ldg_error_string(int status);
 const char* ldg_last_error_message(void);
 int ldg_abi_version(void);

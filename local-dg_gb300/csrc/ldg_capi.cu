@@ -38,6 +38,12 @@ const double kRkA[3] = {0.5, 0.5, 1.0};
 
 }  // namespace
 
+namespace ldg {
+// Lets other translation units of the library report through
+// ldg_last_error_message().
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace ldg
+
 struct ldg_solver {
   ldg_config cfg;
   int N = 0, n = 0, nf = 0, nE = 0;

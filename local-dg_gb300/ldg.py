@@ -31,7 +31,7 @@ LIB = os.path.join(HERE, "libldg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
-SOURCES = ["ldg_capi.cu", "ldg_ops.cpp"]
+SOURCES = ["ldg_capi.cu", "ldg_noalloc.cu", "ldg_ops.cpp"]
 
 LDG_OK = 0
 LDG_HOST = 0
@@ -129,6 +129,7 @@ SIGNATURES = {
     "ldg_enable_kernel_timing": (_i, [_vp, _i]),
     "ldg_kernel_times": (_i, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _i, _i]),
     "ldg_probe_fp64_peak": (_i, [_i, _dp]),
+    "ldg_rhs_noalloc": (_i, [ctypes.POINTER(LdgConfig), _vp, _vp, _vp]),
     "ldg_error_string": (ctypes.c_char_p, [_i]),
     "ldg_last_error_message": (ctypes.c_char_p, []),
     "ldg_abi_version": (_i, []),
