@@ -61,6 +61,15 @@ def fp64_flops_per_element_stage(N: int) -> float:
     return float(grad + rhs)
 
 
+# DRAM bytes (read + write) per element per launch from one ncu capture of
+# the same kernels at 24^3 p=4 (profiles/ncu_k_grad_k_rhs_fp64_tgv24_p4.md),
+# scaled to a launch by the element count (traffic grows with elements).
+NCU_TRAFFIC_PER_ELEMENT = {
+    ("rhs", 5, "fp64"): (608.591872e6 + 192.881408e6) / 13824,
+    ("grad", 5, "fp64"): (116.264960e6 + 271.343104e6) / 13824,
+}
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -274,8 +283,10 @@ def run_ours(args):
     fp64_peak = ldg.probe_fp64_peak(dev)
     flops_step = fp64_flops_per_element_stage(N) * s.nE * 4
     fp64_achieved = flops_step * K / (ms * 1e-3) / 1e12
+    tpe = NCU_TRAFFIC_PER_ELEMENT.get((dom, N, "fp64"))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None,
+                "frac": achieved / hbm_peak, "traffic": tpe * s.nE if tpe else None,
+                "algorithmic_bytes": alg_bytes,
                 "kernel": f"k_rhs<{N}>" if dom == "rhs" else f"k_grad<{N}>",
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
                 "binding_roof": {"pipe": "fp64", "achieved_tflops": fp64_achieved,
