@@ -208,6 +208,63 @@ def run_reference(args):
     return 0
 
 
+def time_steps(s, K, W, dev, pg=None, clocks=False):
+    """W untimed steps, then K timed steps on the solver's stream (CUDA
+    events), per-kernel event timings, optional clock sampling."""
+    import torch
+    stream = torch.cuda.ExternalStream(s.stream, device=dev)
+    for _ in range(W):
+        s.step(1)
+    s.synchronize()
+    s.enable_kernel_timing(True)
+    s.kernel_times(reset=True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(dev) if clocks else None
+    if clk:
+        clk.__enter__()
+    try:
+        e0.record(stream)
+        s.step(K)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    finally:
+        if clk:
+            clk.__exit__(None, None, None)
+    ms = e0.elapsed_time(e1)
+    kt = s.kernel_times(reset=True)
+    s.enable_kernel_timing(False)
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, kt, (clk.summary() if clk else None)
+
+
+def accuracy_vs_fp64(p, nx, steps, dev):
+    """Mixed path against the FP64 path from the same Taylor-Green state:
+    relative L2 state difference after `steps` RK4 steps and the error of
+    the KE-dissipation series (solver.cpp:438-440)."""
+    import numpy as np
+    import ldg
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = ldg.Solver(p, nx, steps=steps, device=dev, precision=prec)
+        s.step(steps)
+        out[prec] = (s.get_state(), s.ke_history(), s.ke_dissipation())
+        s.close()
+    u64, ke64, eps64 = out["fp64"]
+    umx, kemx, epsmx = out["mixed"]
+    return {"steps": steps,
+            "rel_l2_state": float(np.linalg.norm(umx - u64) / np.linalg.norm(u64)),
+            "ke_max_rel_err": float(np.max(np.abs(kemx - ke64) / np.abs(ke64))),
+            "ke_dissipation_max_err_rel": float(np.max(np.abs(epsmx - eps64)) / np.max(np.abs(eps64)))
+            if len(eps64) else None}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -223,33 +280,12 @@ def run_ours(args):
         pg = dist
     ldg.load()
     K, W = args.steps, args.warmup
-    s = ldg.Solver(args.p, args.nx, steps=max(K + W, 1) * 3 + 8, device=dev, check_finite=True)
+    s = ldg.Solver(args.p, args.nx, steps=max(K + W, 1) * 3 + 8, device=dev, check_finite=True,
+                   precision=args.precision)
     n_per_step = s.dofs * s.nE * 4
-    stream = torch.cuda.ExternalStream(s.stream, device=dev)
 
     # ---- device-resident timed region
-    for _ in range(W):
-        s.step(1)
-    s.synchronize()
-    s.enable_kernel_timing(True)
-    s.kernel_times(reset=True)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    if pg:
-        pg.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        e0.record(stream)
-        s.step(K)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    kt = s.kernel_times(reset=True)
-    s.enable_kernel_timing(False)
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, kt, clocks = time_steps(s, K, W, dev, pg, clocks=True)
     value = ws * n_per_step * K / (ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers
@@ -283,35 +319,52 @@ def run_ours(args):
     fp64_peak = ldg.probe_fp64_peak(dev)
     flops_step = fp64_flops_per_element_stage(N) * s.nE * 4
     fp64_achieved = flops_step * K / (ms * 1e-3) / 1e12
-    tpe = NCU_TRAFFIC_PER_ELEMENT.get((dom, N, "fp64"))
+    tpe = NCU_TRAFFIC_PER_ELEMENT.get((dom, N, args.precision))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": tpe * s.nE if tpe else None,
                 "algorithmic_bytes": alg_bytes,
-                "kernel": f"k_rhs<{N}>" if dom == "rhs" else f"k_grad<{N}>",
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "binding_roof": {"pipe": "fp64", "achieved_tflops": fp64_achieved,
-                                 "peak_tflops": fp64_peak, "frac": fp64_achieved / fp64_peak,
-                                 "peak_source": "measured (ldg_probe_fp64_peak FMA chain)",
-                                 "flops_per_dof_stage": fp64_flops_per_element_stage(N) / N ** 3}}
+                "kernel": f"k_rhs<{N},{'double' if args.precision == 'fp64' else 'dd'}>" if dom == "rhs"
+                else f"k_grad<{N}>",
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
+    if args.precision == "fp64":
+        roofline["binding_roof"] = {"pipe": "fp64", "achieved_tflops": fp64_achieved,
+                                    "peak_tflops": fp64_peak, "frac": fp64_achieved / fp64_peak,
+                                    "peak_source": "measured (ldg_probe_fp64_peak FMA chain)",
+                                    "flops_per_dof_stage": fp64_flops_per_element_stage(N) / N ** 3}
     kernel_ms = {k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1)} for k, v in kt.items()}
+    s.close()
+
+    # ---- the mixed-precision variant on the same workload, and its error
+    variants = {}
+    if args.precision == "fp64" and not args.no_variants:
+        sm = ldg.Solver(args.p, args.nx, steps=max(K + W, 1) * 3 + 8, device=dev, precision="mixed")
+        ms_m, kt_m, _ = time_steps(sm, K, W, dev, pg)
+        sm.close()
+        mixed = {"value": ws * n_per_step * K / (ms_m * 1e-3), "ms_per_step": ms_m / K,
+                 "speedup_vs_fp64": ms / ms_m,
+                 "kernels": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kt_m.items()},
+                 "arithmetic": "RHS in FP32-pair (double-word) arithmetic; FP64 state, RK4, reductions"}
+        if args.accuracy_steps > 0:
+            mixed["accuracy_vs_fp64"] = accuracy_vs_fp64(args.p, args.nx, args.accuracy_steps, dev)
+        variants["mixed_f32x2"] = mixed
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (Taylor-Green initial condition, Re=1600, Ma=0.1)",
-        "config": {"workload": f"tgv_{args.nx}^3_p{args.p}_fp64", "nx": args.nx, "p": args.p,
-                   "elements": s.nE, "dofs_per_element": s.dofs, "precision": "fp64",
+        "config": {"workload": f"tgv_{args.nx}^3_p{args.p}_{args.precision}", "nx": args.nx, "p": args.p,
+                   "elements": s.nE, "dofs_per_element": s.dofs, "precision": args.precision,
                    "l2": "inputs larger than L2 (state 1.31 GB at 64^3 p4)" if s.nE * s.dofs * 40 > 129e6
                    else "inputs smaller than L2", "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "e2e": e2e,
         "roofline": roofline,
         "kernels": kernel_ms,
         "gpu_launches": int(kt["grad"][1] + kt["rhs"][1] + kt["reduce"][1]),
-        "clocks": clk.summary(),
+        "clocks": clocks,
+        "variants": variants,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.p)
-    s.close()
     if rank == 0:
         print(json.dumps(line))
     if pg:
@@ -328,6 +381,9 @@ def main():
     ap.add_argument("--nx", type=int, default=64)
     ap.add_argument("--p", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=100)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -52,7 +52,11 @@ extern "C" {
 #define LDG_DEVICE 1
 
 /* arithmetic of the RHS */
-#define LDG_FP64 0  /* every operation in FP64 */
+#define LDG_FP64 0        /* every operation in FP64 */
+#define LDG_MIXED_F32X2 1 /* RHS in FP32-pair ("double-word") arithmetic on
+                             the FP32 pipe; FP64 state, RK4 accumulation,
+                             inverse mass and reductions.  Not bitwise the
+                             reference; error reported against FP64. */
 
 typedef struct ldg_config {
   int p;            /* polynomial order, 1..7 (Solver ctor _p)           */
@@ -65,7 +69,7 @@ typedef struct ldg_config {
   double gamma;     /* ratio of specific heats (solver.cpp:32), 1.4      */
   double Ma;        /* Mach number (solver.cpp:33), default 0.1          */
   double cfl;       /* dt = cfl*min(dx)/(V0(2p+1)) (solver.cpp:47), 0.01 */
-  int precision;    /* LDG_FP64                                          */
+  int precision;    /* LDG_FP64 or LDG_MIXED_F32X2                       */
   int device;       /* CUDA device ordinal                               */
   int check_finite; /* nonzero: ldg_step scans the state for NaN/Inf     */
   int use_box;      /* 0: domain [-pi L, pi L]^3 (driver.cpp:28-31);

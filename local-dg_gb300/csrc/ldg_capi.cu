@@ -50,6 +50,9 @@ struct ldg_solver {
   double dt = 0, tf = 0;
   long long timesteps = 0, step = 0;
   DevOps ops;
+  OpsT<double> o64;  // arithmetic constants of the FP64 path
+  OpsT<dd> odd;      // ... of the FP32-pair (mixed) path
+  bool mixed = false;
   Ops1D o1;
   double xi[kMaxN];  // CGL nodes as the reference computes them
   double lo[3], hi[3];
@@ -163,6 +166,18 @@ int grid_for(int nE) {
   return (nE + Cfg<N>::EPC - 1) / Cfg<N>::EPC;
 }
 
+template <int N, class T>
+cudaError_t set_attrs_t() {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_traces<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_traces<N>())) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_grad<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_grad<N>())) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(k_rhs<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rhs<N>());
+}
+
 template <int N>
 cudaError_t set_attrs() {
   static bool done = false;
@@ -171,21 +186,31 @@ cudaError_t set_attrs() {
   if ((e = cudaFuncSetAttribute(k_transform<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_transform<N>(kNS))) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(k_traces<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_traces<N>())) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_grad<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_grad<N>())) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_rhs<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_rhs<N>())) != cudaSuccess)
-    return e;
   if ((e = cudaFuncSetAttribute(k_ke<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_ke<N>())) != cudaSuccess)
     return e;
+  if ((e = set_attrs_t<N, double>()) != cudaSuccess) return e;
+  if ((e = set_attrs_t<N, dd>()) != cudaSuccess) return e;
   done = true;
   return cudaSuccess;
 }
+
+// Type-erased stage call: pointers to S-typed buffers are void*.
+struct StageCall {
+  const void* Us = nullptr;
+  const void* Q = nullptr;
+  const void* Tu = nullptr;
+  const void* Tq = nullptr;
+  const double* Un = nullptr;
+  double* Uacc = nullptr;
+  void* Unext = nullptr;
+  void* Tu_out = nullptr;
+  double* Kout = nullptr;
+  double* diag = nullptr;
+  int* flag = nullptr;
+  double cacc = 0, cnext = 0;
+  int stage = -1;
+};
 
 template <int N>
 cudaError_t launch_transform(const double* in, double* out, int nE, const DevOps& ops, int inverse,
@@ -193,20 +218,39 @@ cudaError_t launch_transform(const double* in, double* out, int nE, const DevOps
   k_transform<N><<<grid_for<N>(nE), Cfg<N>::T, smem_transform<N>(kNS), st>>>(in, out, nE, kNS, ops, inverse);
   return cudaGetLastError();
 }
-template <int N>
-cudaError_t launch_traces(const double* U, double* Tu, int nE, const DevOps& ops, cudaStream_t st) {
-  k_traces<N><<<grid_for<N>(nE), Cfg<N>::T, smem_traces<N>(), st>>>(U, Tu, nE, ops);
+template <int N, class T>
+cudaError_t launch_traces(const double* U, void* Ucopy, void* Tu, int nE, const OpsT<T>& o, cudaStream_t st) {
+  using S = typename Real<T>::S;
+  k_traces<N, T><<<grid_for<N>(nE), Cfg<N>::T, smem_traces<N>(), st>>>(U, (S*)Ucopy, (S*)Tu, nE, o);
   return cudaGetLastError();
 }
-template <int N>
-cudaError_t launch_grad(const double* U, const double* Tu, double* Q, double* Tq, double* ens,
-                        const DevOps& ops, cudaStream_t st) {
-  k_grad<N><<<grid_for<N>(ops.nE), Cfg<N>::T, smem_grad<N>(), st>>>(U, Tu, Q, Tq, ens, ops);
+template <int N, class T>
+cudaError_t launch_grad(const void* U, const void* Tu, void* Q, void* Tq, double* ens, const DevOps& ops,
+                        const OpsT<T>& o, cudaStream_t st) {
+  using S = typename Real<T>::S;
+  k_grad<N, T><<<grid_for<N>(ops.nE), Cfg<N>::T, smem_grad<N>(), st>>>((const S*)U, (const S*)Tu, (S*)Q,
+                                                                        (S*)Tq, ens, ops, o);
   return cudaGetLastError();
 }
-template <int N>
-cudaError_t launch_rhs(const StageArgs& a, const DevOps& ops, cudaStream_t st) {
-  k_rhs<N><<<grid_for<N>(ops.nE), Cfg<N>::T, smem_rhs<N>(), st>>>(a, ops);
+template <int N, class T>
+cudaError_t launch_rhs(const StageCall& c, const DevOps& ops, const OpsT<T>& o, cudaStream_t st) {
+  using S = typename Real<T>::S;
+  StageArgs<T> a;
+  a.Us = (const S*)c.Us;
+  a.Q = (const S*)c.Q;
+  a.Tu = (const S*)c.Tu;
+  a.Tq = (const S*)c.Tq;
+  a.Un = c.Un;
+  a.Uacc = c.Uacc;
+  a.Unext = (S*)c.Unext;
+  a.Tu_out = (S*)c.Tu_out;
+  a.Kout = c.Kout;
+  a.diag = c.diag;
+  a.flag = c.flag;
+  a.cacc = c.cacc;
+  a.cnext = c.cnext;
+  a.stage = c.stage;
+  k_rhs<N, T><<<grid_for<N>(ops.nE), Cfg<N>::T, smem_rhs<N>(), st>>>(a, ops, o);
   return cudaGetLastError();
 }
 
@@ -230,16 +274,6 @@ cudaError_t launch_ke(const double* U, double* diag, const DevOps& ops, cudaStre
 cudaError_t d_attrs(int N) { LDG_DISPATCH(N, set_attrs<NN>()); }
 cudaError_t d_transform(int N, const double* in, double* out, int nE, const DevOps& ops, int inv, cudaStream_t st) {
   LDG_DISPATCH(N, launch_transform<NN>(in, out, nE, ops, inv, st));
-}
-cudaError_t d_traces(int N, const double* U, double* Tu, int nE, const DevOps& ops, cudaStream_t st) {
-  LDG_DISPATCH(N, launch_traces<NN>(U, Tu, nE, ops, st));
-}
-cudaError_t d_grad(int N, const double* U, const double* Tu, double* Q, double* Tq, double* ens,
-                   const DevOps& ops, cudaStream_t st) {
-  LDG_DISPATCH(N, launch_grad<NN>(U, Tu, Q, Tq, ens, ops, st));
-}
-cudaError_t d_rhs(int N, const StageArgs& a, const DevOps& ops, cudaStream_t st) {
-  LDG_DISPATCH(N, launch_rhs<NN>(a, ops, st));
 }
 cudaError_t d_ke(int N, const double* U, double* diag, const DevOps& ops, cudaStream_t st) {
   LDG_DISPATCH(N, launch_ke<NN>(U, diag, ops, st));
@@ -333,10 +367,25 @@ __global__ void k_fp64_chain(double* out, int iters) {
   if (r == 1234.5) out[0] = r;  // keeps the chain live; never true
 }
 
-// nodal (reference layout, in s->nodal) -> Un, and traces of Un
+// Stage kernels in the solver's arithmetic (mixed: FP32 pairs) or FP64.
+cudaError_t s_traces(ldg_solver* s, bool mixed, const double* U, void* Ucopy, void* Tu) {
+  if (mixed) LDG_DISPATCH(s->N, (launch_traces<NN, dd>(U, Ucopy, Tu, s->nE, s->odd, s->stream)));
+  LDG_DISPATCH(s->N, (launch_traces<NN, double>(U, Ucopy, Tu, s->nE, s->o64, s->stream)));
+}
+cudaError_t s_grad(ldg_solver* s, bool mixed, const void* U, const void* Tu, double* ens) {
+  if (mixed) LDG_DISPATCH(s->N, (launch_grad<NN, dd>(U, Tu, s->Q, s->Tq, ens, s->ops, s->odd, s->stream)));
+  LDG_DISPATCH(s->N, (launch_grad<NN, double>(U, Tu, s->Q, s->Tq, ens, s->ops, s->o64, s->stream)));
+}
+cudaError_t s_rhs(ldg_solver* s, bool mixed, const StageCall& c) {
+  if (mixed) LDG_DISPATCH(s->N, (launch_rhs<NN, dd>(c, s->ops, s->odd, s->stream)));
+  LDG_DISPATCH(s->N, (launch_rhs<NN, double>(c, s->ops, s->o64, s->stream)));
+}
+
+// nodal (reference layout, in s->nodal) -> Un and the traces of Un; on the
+// mixed path also the FP32-pair copy of Un in Us (the stage-0 input).
 int load_state_from_nodal(ldg_solver* s) {
   LDG_CUDA(d_transform(s->N, s->nodal, s->Un, s->nE, s->ops, 0, s->stream));
-  LDG_CUDA(d_traces(s->N, s->Un, s->Tu[s->cur], s->nE, s->ops, s->stream));
+  LDG_CUDA(s_traces(s, s->mixed, s->Un, s->mixed ? (void*)s->Us : nullptr, s->Tu[s->cur]));
   return LDG_OK;
 }
 
@@ -408,7 +457,8 @@ int ldg_create(const ldg_config* cfg, ldg_solver** out) {
     return fail(LDG_ERR_INVALID, "each direction needs at least 3 elements");
   if (!(c.tf > 0) || !(c.Re > 0) || !(c.Pr > 0) || !(c.gamma > 1) || !(c.Ma > 0) || !(c.cfl > 0) || !(c.L > 0))
     return fail(LDG_ERR_INVALID, "physical parameters must be positive (gamma > 1)");
-  if (c.precision != LDG_FP64) return fail(LDG_ERR_UNSUPPORTED, "precision mode not built");
+  if (c.precision != LDG_FP64 && c.precision != LDG_MIXED_F32X2)
+    return fail(LDG_ERR_UNSUPPORTED, "precision mode not built");
   if ((long long)c.nx * c.ny * c.nz > 0x7fffffffLL / 8) return fail(LDG_ERR_INVALID, "mesh too large");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -485,6 +535,9 @@ int ldg_create(const ldg_config* cfg, ldg_solver** out) {
   o.ny = c.ny;
   o.nz = c.nz;
   o.nE = s->nE;
+  s->o64 = make_opst<double>(o, N);
+  s->odd = make_opst<dd>(o, N);
+  s->mixed = c.precision == LDG_MIXED_F32X2;
 
   int st;
   if (cudaSetDevice(c.device) != cudaSuccess) {
@@ -602,21 +655,29 @@ int ldg_rhs(ldg_solver* s, const double* u_curr, double* k, int where) {
   LDG_CUDA(cudaSetDevice(s->cfg.device));
   int st = copy_in(s, s->nodal, u_curr, state_count(s), where);
   if (st) return st;
-  // Work in the stage buffers so the solver state (Un, Tu[cur]) is kept.
+  // Work in scratch buffers so the solver state (Un, Us, Tu[cur]) is kept:
+  // the FP64 input goes to Uacc, the stage-input copy to the nodal buffer.
   double* Tu = s->Tu[1 - s->cur];
-  LDG_CUDA(d_transform(s->N, s->nodal, s->Us, s->nE, s->ops, 0, s->stream));
-  LDG_CUDA(d_traces(s->N, s->Us, Tu, s->nE, s->ops, s->stream));
-  LDG_CUDA(d_grad(s->N, s->Us, Tu, s->Q, s->Tq, nullptr, s->ops, s->stream));
-  StageArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.Us = s->Us;
-  a.Q = s->Q;
-  a.Tu = Tu;
-  a.Tq = s->Tq;
-  a.Kout = s->Uacc;
-  a.stage = -1;
-  LDG_CUDA(d_rhs(s->N, a, s->ops, s->stream));
-  LDG_CUDA(d_transform(s->N, s->Uacc, s->nodal, s->nE, s->ops, 1, s->stream));
+  LDG_CUDA(d_transform(s->N, s->nodal, s->Uacc, s->nE, s->ops, 0, s->stream));
+  const void* Uin = s->Uacc;
+  if (s->mixed) {
+    LDG_CUDA(s_traces(s, true, s->Uacc, s->nodal, Tu));
+    Uin = s->nodal;
+  } else {
+    LDG_CUDA(s_traces(s, false, s->Uacc, nullptr, Tu));
+  }
+  LDG_CUDA(s_grad(s, s->mixed, Uin, Tu, nullptr));
+  StageCall c;
+  c.Us = Uin;
+  c.Q = s->Q;
+  c.Tu = Tu;
+  c.Tq = s->Tq;
+  c.Kout = s->Us;  // FP64 RHS in the stage buffer (restored below on the mixed path)
+  c.stage = -1;
+  LDG_CUDA(s_rhs(s, s->mixed, c));
+  LDG_CUDA(d_transform(s->N, s->Us, s->nodal, s->nE, s->ops, 1, s->stream));
+  if (s->mixed)  // Us held the pair copy of Un: rebuild it
+    LDG_CUDA(s_traces(s, true, s->Un, s->Us, s->Tu[1 - s->cur]));
   return copy_out(s, k, s->nodal, state_count(s), where);
 }
 
@@ -628,33 +689,39 @@ int ldg_step(ldg_solver* s, int nsteps) {
   int st = ensure_ke_capacity(s, s->step + nsteps + 1);
   if (st) return st;
   if (s->cfg.check_finite) LDG_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
-  const int N = s->N;
+  const bool mixed = s->mixed;
   for (int it = 0; it < nsteps; ++it) {
     const int cur = s->cur;
     for (int stage = 0; stage < 4; ++stage) {
-      const double* Uin = stage == 0 ? s->Un : s->Us;
+      // Stage input: the FP64 state on the FP64 path at stage 0, otherwise
+      // the stage buffer (on the mixed path it holds the FP32-pair copy).
+      const void* Uin = (stage == 0 && !mixed) ? (const void*)s->Un : (const void*)s->Us;
       double* Tu_in = s->Tu[(stage & 1) ? 1 - cur : cur];
       double* Tu_out = s->Tu[(stage & 1) ? cur : 1 - cur];
       LDG_CUDA(tic(s, 0));
-      LDG_CUDA(d_grad(N, Uin, Tu_in, s->Q, s->Tq, nullptr, s->ops, s->stream));
+      LDG_CUDA(s_grad(s, mixed, Uin, Tu_in, nullptr));
       LDG_CUDA(toc(s));
-      StageArgs a;
-      std::memset(&a, 0, sizeof(a));
-      a.Us = Uin;
-      a.Q = s->Q;
-      a.Tu = Tu_in;
-      a.Tq = s->Tq;
-      a.Un = s->Un;
-      a.Uacc = s->Uacc;
-      a.Unext = stage < 3 ? s->Us : nullptr;
-      a.Tu_out = Tu_out;
-      a.diag = stage == 3 ? s->diag : nullptr;
-      a.flag = s->cfg.check_finite ? s->flag : nullptr;
-      a.cacc = s->dt * kRkB[stage];
-      a.cnext = stage < 3 ? s->dt * kRkA[stage] : 0.0;
-      a.stage = stage;
+      StageCall c;
+      c.Us = Uin;
+      c.Q = s->Q;
+      c.Tu = Tu_in;
+      c.Tq = s->Tq;
+      c.Un = s->Un;
+      c.Uacc = s->Uacc;
+      c.Unext = (stage < 3 || mixed) ? (void*)s->Us : nullptr;
+      c.Tu_out = Tu_out;
+      c.diag = (stage == 3 && !mixed) ? s->diag : nullptr;
+      c.flag = s->cfg.check_finite ? s->flag : nullptr;
+      c.cacc = s->dt * kRkB[stage];
+      c.cnext = stage < 3 ? s->dt * kRkA[stage] : 0.0;
+      c.stage = stage;
       LDG_CUDA(tic(s, 1));
-      LDG_CUDA(d_rhs(N, a, s->ops, s->stream));
+      LDG_CUDA(s_rhs(s, mixed, c));
+      LDG_CUDA(toc(s));
+    }
+    if (mixed) {  // computeKE of the new FP64 state
+      LDG_CUDA(tic(s, 2));
+      LDG_CUDA(d_ke(s->N, s->Uacc, s->diag, s->ops, s->stream));
       LDG_CUDA(toc(s));
     }
     // After four stages Tu[cur] holds the traces of Uacc = u^{n+1}.
@@ -691,8 +758,11 @@ int ldg_time_step(ldg_solver* s) {
 int ldg_diagnostics(ldg_solver* s, double* ke_ref, double* ke, double* enstrophy) {
   if (!s) return fail(LDG_ERR_INVALID, "null solver");
   LDG_CUDA(cudaSetDevice(s->cfg.device));
-  // Enstrophy from the LDG gradient of the current state; KE from Un.
-  LDG_CUDA(d_grad(s->N, s->Un, s->Tu[s->cur], s->Q, s->Tq, s->ens, s->ops, s->stream));
+  // Enstrophy from the FP64 LDG gradient of the current state (traces
+  // rebuilt in FP64 in the spare trace buffer); KE from Un.
+  double* Tu = s->Tu[1 - s->cur];
+  LDG_CUDA(s_traces(s, false, s->Un, nullptr, Tu));
+  LDG_CUDA(s_grad(s, false, s->Un, Tu, s->ens));
   LDG_CUDA(d_ke(s->N, s->Un, s->diag, s->ops, s->stream));
   k_reduce<<<1, 1024, 0, s->stream>>>(s->diag, s->nE, 2, 0, s->ops.ke_norm, s->red + 0);
   k_reduce<<<1, 1024, 0, s->stream>>>(s->diag, s->nE, 2, 1, s->ops.ke_norm, s->red + 1);

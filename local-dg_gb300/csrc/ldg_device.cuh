@@ -1,5 +1,6 @@
-// Device-side pieces shared by the LDG kernels: operator block, mesh
-// neighbour map, pointwise fluxes.
+// Device-side pieces shared by the LDG kernels: operator blocks, mesh
+// neighbour map, pointwise fluxes (templated on the arithmetic type T =
+// double or dd, see ldg_real.cuh).
 //
 // Pointwise physics restated from Local-DG solver.cpp (fluxC 1040-1086,
 // fluxV 1089-1188, numericalFluxC 1194-1374, numericalFluxV 891-921,
@@ -9,13 +10,19 @@
 #pragma once
 #include <cstdint>
 
+#include "ldg_real.cuh"
+
 namespace ldg {
+
+using ::fabs;
+using ::fma;
+using ::sqrt;
 
 constexpr int kNS = 5;     // conserved variables (solver.cpp:61)
 constexpr int kNQ = 15;    // gradient components: 3 directions x 5 vars
 constexpr int kDevMaxN = 8;
 
-// Everything a kernel needs about the discretisation; passed by value.
+// Double-precision operator block and mesh geometry; passed by value.
 struct DevOps {
   double A[kDevMaxN * kDevMaxN];   // weak derivative, A[q*N + r]
   double B[kDevMaxN * kDevMaxN];   // CGL nodal -> Gauss, B[q*N + i]
@@ -32,6 +39,41 @@ struct DevOps {
   double ke_norm;                     // 1 / (rho0 (2 pi L)^3)
   int nx, ny, nz, nE;
 };
+
+// The arithmetic constants of the step kernels in the type they compute in.
+template <class T>
+struct OpsT {
+  T A[kDevMaxN * kDevMaxN];
+  T lp[kDevMaxN], lm[kDevMaxN], Lp[kDevMaxN], Lm[kDevMaxN];
+  T ia[3];
+  T g1, hg1, gamma, inv_re, kappa, two3, one;
+};
+
+// Host-side conversion of the double block into the arithmetic type T.
+inline double host_cast(double v, const double*) { return v; }
+inline dd host_cast(double v, const dd*) { return dd_from_host(v); }
+
+template <class T>
+inline OpsT<T> make_opst(const DevOps& d, int N) {
+  OpsT<T> o;
+  const T* tag = nullptr;
+  for (int i = 0; i < kDevMaxN * kDevMaxN; ++i) o.A[i] = host_cast(i < N * N ? d.A[i] : 0.0, tag);
+  for (int i = 0; i < kDevMaxN; ++i) {
+    o.lp[i] = host_cast(d.lp[i], tag);
+    o.lm[i] = host_cast(d.lm[i], tag);
+    o.Lp[i] = host_cast(d.Lp[i], tag);
+    o.Lm[i] = host_cast(d.Lm[i], tag);
+  }
+  for (int l = 0; l < 3; ++l) o.ia[l] = host_cast(d.ia[l], tag);
+  o.g1 = host_cast(d.g1, tag);
+  o.hg1 = host_cast(0.5 * d.g1, tag);
+  o.gamma = host_cast(d.gamma, tag);
+  o.inv_re = host_cast(d.inv_re, tag);
+  o.kappa = host_cast(d.kappa, tag);
+  o.two3 = host_cast(2.0 / 3.0, tag);
+  o.one = host_cast(1.0, tag);
+  return o;
+}
 
 // Periodic face neighbour: element numbering e = ix + nx (iy + ny iz)
 // (mesh.cpp:162); faces -x,+x,-y,+y,-z,+z.  On one rank the reference's
@@ -58,27 +100,36 @@ __device__ __forceinline__ bool not_finite(double x) {
   return (__double_as_longlong(x) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
 }
 
+// helpers that are exact in both types
+__device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ double half_(double x) { return 0.5 * x; }
+__device__ __forceinline__ dd half_(dd x) { return scale2(x, 0.5f); }
+template <class T>
+__device__ __forceinline__ T sgn(bool plus, T x) { return plus ? x : -x; }
+
 // Euler flux, column l of F(u): components (rho, m_x, m_y, m_z, E) of the
 // flux in direction l (solver.cpp:1060-1084 with fluxes[iS + 5 l]).
 // ir = 1/rho; p = g1 (E - |m|^2/(2 rho)); energy flux m_l (E + p)/rho, with
 // E + p written gamma E - g1|m|^2/(2rho) as the reference does.
+template <class T>
 struct Euler {
-  double ir, p, h;  // 1/rho, pressure, (E+p)/rho
+  T ir, p, h;  // 1/rho, pressure, (E+p)/rho
 };
 
-__device__ __forceinline__ Euler euler_state(const double u[kNS], double g1, double gamma) {
-  Euler s;
-  s.ir = 1.0 / u[0];
-  double k = (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) * s.ir * (0.5 * g1);
-  s.p = g1 * u[4] - k;
-  s.h = (gamma * u[4] - k) * s.ir;
+template <class T>
+__device__ __forceinline__ Euler<T> euler_state(const T u[kNS], const OpsT<T>& o) {
+  Euler<T> s;
+  s.ir = rcp(u[0]);
+  T k = (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) * s.ir * o.hg1;
+  s.p = o.g1 * u[4] - k;
+  s.h = (o.gamma * u[4] - k) * s.ir;
   return s;
 }
 
-__device__ __forceinline__ void euler_column(const double u[kNS], const Euler& s, int l,
-                                             double F[kNS]) {
-  double ml = u[1 + l];
-  double vl = ml * s.ir;
+template <class T>
+__device__ __forceinline__ void euler_column(const T u[kNS], const Euler<T>& s, int l, T F[kNS]) {
+  T ml = u[1 + l];
+  T vl = ml * s.ir;
   F[0] = ml;
   F[1] = u[1] * vl;
   F[2] = u[2] * vl;
@@ -90,22 +141,24 @@ __device__ __forceinline__ void euler_column(const double u[kNS], const Euler& s
 // Velocity gradient G[i][j] = d_j v_i from u and Du[c], c = j*5 + var
 // (the chain rule of solver.cpp:1137-1170), plus d_j e with
 // e = E/rho - |v|^2/2 the specific internal energy.
+template <class T>
 struct ViscPre {
-  double v[3];
-  double G[3][3];
-  double de[3];
-  double div;
+  T v[3];
+  T G[3][3];
+  T de[3];
+  T div;
 };
 
-__device__ __forceinline__ void visc_pre(const double u[kNS], const double* Du, ViscPre& P) {
-  double ir = 1.0 / u[0];
+template <class T>
+__device__ __forceinline__ void visc_pre(const T u[kNS], const T* Du, ViscPre<T>& P) {
+  T ir = rcp(u[0]);
   P.v[0] = u[1] * ir;
   P.v[1] = u[2] * ir;
   P.v[2] = u[3] * ir;
-  double eo = u[4] * ir;
+  T eo = u[4] * ir;
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    double dr = Du[j * kNS + 0];
+    T dr = Du[j * kNS + 0];
 #pragma unroll
     for (int i = 0; i < 3; ++i) P.G[i][j] = (Du[j * kNS + 1 + i] - dr * P.v[i]) * ir;
     P.de[j] = (Du[j * kNS + 4] - dr * eo) * ir -
@@ -116,61 +169,59 @@ __device__ __forceinline__ void visc_pre(const double u[kNS], const double* Du, 
 
 // Column j of the viscous flux (solver.cpp:1136-1187): Newtonian stress with
 // Stokes' hypothesis over Re, heat flux (gamma/Pr) grad e / Re.
-template <int j>
-__device__ __forceinline__ void visc_column(const ViscPre& P, double inv_re,
-                                            double kappa, double F[kNS]) {
-  double tau[3];
+template <int j, class T>
+__device__ __forceinline__ void visc_column(const ViscPre<T>& P, const OpsT<T>& o, T F[kNS]) {
+  T tau[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) tau[i] = P.G[i][j] + P.G[j][i];
-  tau[j] -= (2.0 / 3.0) * P.div;
-  F[0] = 0.0;
-  F[1] = tau[0] * inv_re;
-  F[2] = tau[1] * inv_re;
-  F[3] = tau[2] * inv_re;
-  F[4] = (tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + kappa * P.de[j]) * inv_re;
+  tau[j] -= o.two3 * P.div;
+  F[0] = T{};
+  F[1] = tau[0] * o.inv_re;
+  F[2] = tau[1] * o.inv_re;
+  F[3] = tau[2] * o.inv_re;
+  F[4] = (tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + o.kappa * P.de[j]) * o.inv_re;
 }
 
 // Roe flux F*(uN, uK, n) seen from element K with n = s e_l
 // (numericalFluxC, solver.cpp:1291-1372): central flux minus Roe-averaged
 // upwind dissipation; the reference's hard-coded 0.4 is g1.
-template <int l>
-__device__ __forceinline__ void roe_flux(const double uN[kNS], const double uK[kNS], double s,
-                                         double g1, double F[kNS]) {
-  double rN = uN[0], rK = uK[0];
-  double irN = 1.0 / rN, irK = 1.0 / rK;
-  double vN[3] = {uN[1] * irN, uN[2] * irN, uN[3] * irN};
-  double vK[3] = {uK[1] * irK, uK[2] * irK, uK[3] * irK};
-  double qN = s * vN[l], qK = s * vK[l];
-  double pN = g1 * uN[4] - (0.5 * g1) * rN * (vN[0] * vN[0] + vN[1] * vN[1] + vN[2] * vN[2]);
-  double pK = g1 * uK[4] - (0.5 * g1) * rK * (vK[0] * vK[0] + vK[1] * vK[1] + vK[2] * vK[2]);
-  double sq = sqrt(rN * irK);
-  double is1 = 1.0 / (sq + 1.0);
-  double vt[3];
+template <int l, class T>
+__device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool s, const OpsT<T>& o,
+                                         T F[kNS]) {
+  T rN = uN[0], rK = uK[0];
+  T irN = rcp(rN), irK = rcp(rK);
+  T vN[3] = {uN[1] * irN, uN[2] * irN, uN[3] * irN};
+  T vK[3] = {uK[1] * irK, uK[2] * irK, uK[3] * irK};
+  T qN = sgn(s, vN[l]), qK = sgn(s, vK[l]);
+  T pN = o.g1 * uN[4] - o.hg1 * rN * (vN[0] * vN[0] + vN[1] * vN[1] + vN[2] * vN[2]);
+  T pK = o.g1 * uK[4] - o.hg1 * rK * (vK[0] * vK[0] + vK[1] * vK[1] + vK[2] * vK[2]);
+  T sq = sqrt(rN * irK);
+  T is1 = rcp(sq + o.one);
+  T vt[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) vt[i] = (sq * vN[i] + vK[i]) * is1;
-  double Ht = (sq * (uN[4] + pN) * irN + (uK[4] + pK) * irK) * is1;
-  double vt2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
-  double qt = s * vt[l];
-  double c2 = g1 * (Ht - 0.5 * vt2);
-  double ic2 = 1.0 / c2;
-  double c = sqrt(c2);
-  double ic = c * ic2;  // 1/c
-  double l0 = fabs(qt);
-  double lp = 0.5 * fabs(qt + c), lm = 0.5 * fabs(c - qt);
-  double dr = rN - rK;
-  double dm[3] = {uN[1] - uK[1], uN[2] - uK[2], uN[3] - uK[3]};
-  double dE = uN[4] - uK[4];
-  double a1 = lp + lm - l0, a2 = lp - lm;
-  double dp = g1 * (0.5 * vt2 * dr - (vt[0] * dm[0] + vt[1] * dm[1] + vt[2] * dm[2]) + dE);
-  double dq = -qt * dr + s * dm[l];
-  double t179 = a1 * dp * ic2 + a2 * dq * ic;
-  double t186 = a2 * dp * ic + a1 * dq;
-  F[0] = 0.5 * (rN * qN + rK * qK - l0 * dr - t179);
+  T Ht = (sq * (uN[4] + pN) * irN + (uK[4] + pK) * irK) * is1;
+  T vt2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
+  T qt = sgn(s, vt[l]);
+  T c2 = o.g1 * (Ht - half_(vt2));
+  T ic2 = rcp(c2);
+  T c = sqrt(c2);
+  T ic = c * ic2;  // 1/c
+  T l0 = fabs(qt);
+  T lp = half_(fabs(qt + c)), lm = half_(fabs(c - qt));
+  T dr = rN - rK;
+  T dm[3] = {uN[1] - uK[1], uN[2] - uK[2], uN[3] - uK[3]};
+  T dE = uN[4] - uK[4];
+  T a1 = lp + lm - l0, a2 = lp - lm;
+  T dp = o.g1 * (half_(vt2) * dr - (vt[0] * dm[0] + vt[1] * dm[1] + vt[2] * dm[2]) + dE);
+  T dq = sgn(s, dm[l]) - qt * dr;
+  T t179 = a1 * dp * ic2 + a2 * dq * ic;
+  T t186 = a2 * dp * ic + a1 * dq;
+  F[0] = half_(rN * qN + rK * qK - l0 * dr - t179);
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
-    F[1 + i] = 0.5 * (uN[1 + i] * qN + uK[1 + i] * qK - l0 * dm[i] - t179 * vt[i]);
-  F[1 + l] += 0.5 * s * (pN + pK - t186);
-  F[4] = 0.5 * ((uN[4] + pN) * qN + (uK[4] + pK) * qK - l0 * dE - t179 * Ht - t186 * qt);
+  for (int i = 0; i < 3; ++i) F[1 + i] = half_(uN[1 + i] * qN + uK[1 + i] * qK - l0 * dm[i] - t179 * vt[i]);
+  F[1 + l] += half_(sgn(s, pN + pK - t186));
+  F[4] = half_((uN[4] + pN) * qN + (uK[4] + pK) * qK - l0 * dE - t179 * Ht - t186 * qt);
 }
 
 }  // namespace ldg

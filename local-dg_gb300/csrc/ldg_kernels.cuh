@@ -1,4 +1,5 @@
-// FP64 LDG kernels, templated on N = p + 1.
+// LDG kernels, templated on N = p + 1 and on the arithmetic type T
+// (double: the FP64 path; dd: FP32-pair arithmetic of the mixed path).
 //
 // State layout in HBM ("Gauss space"): U[e][var][q], q = qx + N qy + N^2 qz,
 // the values of the element's polynomial at the tensor Gauss points.  This
@@ -8,22 +9,26 @@
 // J * diag(w) (it is exact in both bases).  The conversions to and from the
 // reference's nodal layout are k_transform below.
 //
-// Buffers per element:
-//   U   [5][n]          state (and stage input, RK accumulator)
-//   Q   [15][n]         LDG gradient q = grad u, c = l*5 + var
-//   Tu  [6][5][nf]      face traces of U on the six faces
-//   Tq  [3][15][nf]     traces of Q on the three minus faces (the only ones
+// Buffers per element (S = double on the FP64 path, float2 pairs on the
+// mixed path; 8 bytes per value either way):
+//   Un, Uacc [5][n]     state and RK accumulator, always FP64
+//   Us   [5][n]  (S)    stage input state
+//   Q    [15][n] (S)    LDG gradient q = grad u, c = l*5 + var
+//   Tu   [6][5][nf] (S) face traces of the stage state on the six faces
+//   Tq   [3][15][nf] (S) traces of Q on the three minus faces (the only ones
 //                       the alternating LDG fluxes read)
 // with n = N^3, nf = N^2.  Face point t = a + N b over the face's two
 // tangential directions in increasing order (mesh.cpp:428-501).
 //
 // One CTA works on EPC elements with one thread per (element, Gauss
-// point); face work is spread over all threads.  The kernels are FP64-pipe
-// bound on GB300, so the layout choices minimise FP64 operations:
+// point); face work is spread over all threads.  The FP64 kernels are
+// FP64-pipe bound on GB300, so the layout choices minimise arithmetic:
 // traces are written once by the producer of a state and read (not
 // recomputed) by both neighbours, and the mass matrix inverse is folded
 // into the 1-D operators.
 #pragma once
+#include <type_traits>
+
 #include "ldg_device.cuh"
 
 namespace ldg {
@@ -57,7 +62,7 @@ __device__ __forceinline__ int tangential(int l, int qx, int qy, int qz) {
 
 // ---------------------------------------------------------------------------
 // Tensor transform per element: out = (M x M x M) in for nv components,
-// M row major N x N (B: nodal -> Gauss, Bi: Gauss -> nodal).
+// M row major N x N (B: nodal -> Gauss, Bi: Gauss -> nodal).  FP64.
 template <int N>
 __global__ void __launch_bounds__(Cfg<N>::T) k_transform(const double* __restrict__ in,
                                                          double* __restrict__ out, int nE, int nv,
@@ -100,38 +105,48 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_transform(const double* __restric
 }
 
 // ---------------------------------------------------------------------------
-// Face traces of a state: Tu[e][f][v][t] = sum_qn l_{+-}[qn] U[e][v][pt].
-template <int N>
-__device__ __forceinline__ void write_traces(const double* sU, int ne, long e0, double* Tu,
-                                             const DevOps& ops) {
-  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, T = Cfg<N>::T;
-  for (int i = threadIdx.x; i < ne * 6 * kNS * nf; i += T) {
+// Face traces of a state held in shared memory:
+// Tu[e][f][v][t] = sum_qn l_{+-}[qn] U[e][v][pt].
+template <int N, class T>
+__device__ __forceinline__ void write_traces(const T* sU, int ne, long e0, typename Real<T>::S* Tu,
+                                             const OpsT<T>& o) {
+  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, NT = Cfg<N>::T;
+  for (int i = threadIdx.x; i < ne * 6 * kNS * nf; i += NT) {
     int es = i / (6 * kNS * nf);
     int r = i - es * 6 * kNS * nf;
     int f = r / (kNS * nf);
     int r2 = r - f * kNS * nf;
     int v = r2 / nf, t = r2 - v * nf;
     int l = f >> 1;
-    const double* lvec = (f & 1) ? ops.lp : ops.lm;
+    const T* lvec = (f & 1) ? o.lp : o.lm;
     const int st = stride_of<N>(l);
-    const double* row = sU + (es * kNS + v) * n + face_point<N>(l, 0, t);
-    double acc = 0.0;
+    const T* row = sU + (es * kNS + v) * n + face_point<N>(l, 0, t);
+    T acc{};
 #pragma unroll
     for (int qn = 0; qn < N; ++qn) acc = fma(lvec[qn], row[qn * st], acc);
-    Tu[(e0 + es) * 6 * kNS * nf + r] = acc;
+    Real<T>::st(Tu + (e0 + es) * 6 * kNS * nf + r, acc);
   }
 }
 
-template <int N>
+// Traces of an FP64 state; on the mixed path also writes the FP32-pair copy
+// of the state (Ucopy) that the stage kernels read.
+template <int N, class T>
 __global__ void __launch_bounds__(Cfg<N>::T) k_traces(const double* __restrict__ U,
-                                                      double* __restrict__ Tu, int nE, const __grid_constant__ DevOps ops) {
-  constexpr int n = Cfg<N>::n, EPC = Cfg<N>::EPC, T = Cfg<N>::T;
-  extern __shared__ double smem[];
+                                                      typename Real<T>::S* __restrict__ Ucopy,
+                                                      typename Real<T>::S* __restrict__ Tu, int nE,
+                                                      const __grid_constant__ OpsT<T> o) {
+  constexpr int n = Cfg<N>::n, EPC = Cfg<N>::EPC, NT = Cfg<N>::T;
+  extern __shared__ double smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
   const long e0 = (long)blockIdx.x * EPC;
   const int ne = (int)min((long)EPC, nE - e0);
-  for (int i = threadIdx.x; i < ne * kNS * n; i += T) smem[i] = U[e0 * kNS * n + i];
+  for (int i = threadIdx.x; i < ne * kNS * n; i += NT) {
+    T v = Real<T>::from_f64(U[e0 * kNS * n + i]);
+    smem[i] = v;
+    if (Ucopy) Real<T>::st(Ucopy + e0 * kNS * n + i, v);
+  }
   __syncthreads();
-  write_traces<N>(smem, ne, e0, Tu, ops);
+  write_traces<N, T>(smem, ne, e0, Tu, o);
 }
 
 // ---------------------------------------------------------------------------
@@ -139,103 +154,110 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_traces(const double* __restrict__
 //   Q_l = (1/alpha_l) [ -A_l U + Lp (x) tr(+l, own) - Lm (x) tr(+l, -l neighbour) ]
 // The one-sided flux numericalFluxL takes u from the element on the minus
 // side of every face, so only plus-face traces are read.
-// Writes Q and the minus-face traces Tq; optionally per-element enstrophy.
-template <int N>
-__global__ void __launch_bounds__(Cfg<N>::T) k_grad(const double* __restrict__ U,
-                                                    const double* __restrict__ Tu,
-                                                    double* __restrict__ Q,
-                                                    double* __restrict__ Tq,
-                                                    double* __restrict__ ens, const __grid_constant__ DevOps ops) {
-  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, EPC = Cfg<N>::EPC, T = Cfg<N>::T;
-  extern __shared__ double smem[];
-  double* sU = smem;                       // EPC*5*n
-  double* sQ = sU + EPC * kNS * n;         // EPC*15*n
-  double* sTp = sQ + EPC * kNQ * n;        // EPC*3*5*nf  own +l traces
-  double* sTm = sTp + EPC * 3 * kNS * nf;  // EPC*3*5*nf  (-l neighbour)'s +l traces
-  double* sE = sTm + EPC * 3 * kNS * nf;   // EPC*n       enstrophy density
+// Writes Q and the minus-face traces Tq; on the FP64 path optionally the
+// per-element enstrophy.
+template <int N, class T>
+__global__ void __launch_bounds__(Cfg<N>::T) k_grad(const typename Real<T>::S* __restrict__ U,
+                                                    const typename Real<T>::S* __restrict__ Tu,
+                                                    typename Real<T>::S* __restrict__ Q,
+                                                    typename Real<T>::S* __restrict__ Tq,
+                                                    double* __restrict__ ens,
+                                                    const __grid_constant__ DevOps ops,
+                                                    const __grid_constant__ OpsT<T> o) {
+  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, EPC = Cfg<N>::EPC, NT = Cfg<N>::T;
+  using R = Real<T>;
+  extern __shared__ double smem_raw[];
+  T* sU = reinterpret_cast<T*>(smem_raw);  // EPC*5*n
+  T* sQ = sU + EPC * kNS * n;              // EPC*15*n
+  T* sTp = sQ + EPC * kNQ * n;             // EPC*3*5*nf  own +l traces
+  T* sTm = sTp + EPC * 3 * kNS * nf;       // EPC*3*5*nf  (-l neighbour)'s +l traces
+  double* sE = reinterpret_cast<double*>(sTm + EPC * 3 * kNS * nf);  // EPC*n enstrophy
   const int nE = ops.nE;
   const long e0 = (long)blockIdx.x * EPC;
   const int ne = (int)min((long)EPC, nE - e0);
-  for (int i = threadIdx.x; i < ne * kNS * n; i += T) sU[i] = U[e0 * kNS * n + i];
-  for (int i = threadIdx.x; i < ne * 3 * kNS * nf; i += T) {
+  for (int i = threadIdx.x; i < ne * kNS * n; i += NT) sU[i] = R::ld(U + e0 * kNS * n + i);
+  for (int i = threadIdx.x; i < ne * 3 * kNS * nf; i += NT) {
     int es = i / (3 * kNS * nf);
     int r = i - es * 3 * kNS * nf;
     int l = r / (kNS * nf);
     int r2 = r - l * kNS * nf;
     long e = e0 + es;
     int en = face_neighbour((int)e, 2 * l, ops.nx, ops.ny, ops.nz);
-    sTp[i] = Tu[(e * 6 + 2 * l + 1) * kNS * nf + r2];
-    sTm[i] = Tu[((long)en * 6 + 2 * l + 1) * kNS * nf + r2];
+    sTp[i] = R::ld(Tu + (e * 6 + 2 * l + 1) * kNS * nf + r2);
+    sTm[i] = R::ld(Tu + ((long)en * 6 + 2 * l + 1) * kNS * nf + r2);
   }
   __syncthreads();
   const int es = threadIdx.x / n, q = threadIdx.x % n;
   if (es < ne) {
     const int c[3] = {q % N, (q / N) % N, q / (N * N)};
-    double grad[kNQ];
+    T grad[kNQ];
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
       const int qn = c[l];
       const int st = stride_of<N>(l);
       const int b = q - qn * st;
       const int t = tangential<N>(l, c[0], c[1], c[2]);
-      double row[N];
+      T row[N];
 #pragma unroll
-      for (int r = 0; r < N; ++r) row[r] = ops.A[qn * N + r];
-      const double lp = ops.Lp[qn], lm = ops.Lm[qn], ia = ops.ia[l];
+      for (int r = 0; r < N; ++r) row[r] = o.A[qn * N + r];
+      const T lp = o.Lp[qn], lm = o.Lm[qn], ia = o.ia[l];
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
-        const double* line = sU + (es * kNS + v) * n + b;
-        double acc = 0.0;
+        const T* line = sU + (es * kNS + v) * n + b;
+        T acc{};
 #pragma unroll
         for (int r = 0; r < N; ++r) acc = fma(row[r], line[r * st], acc);
-        const double tp = sTp[((es * 3 + l) * kNS + v) * nf + t];
-        const double tm = sTm[((es * 3 + l) * kNS + v) * nf + t];
-        const double g = (lp * tp - lm * tm - acc) * ia;
+        const T tp = sTp[((es * 3 + l) * kNS + v) * nf + t];
+        const T tm = sTm[((es * 3 + l) * kNS + v) * nf + t];
+        const T g = (lp * tp - lm * tm - acc) * ia;
         grad[l * kNS + v] = g;
         sQ[(es * kNQ + l * kNS + v) * n + q] = g;
-        Q[((e0 + es) * kNQ + l * kNS + v) * n + q] = g;
+        R::st(Q + ((e0 + es) * kNQ + l * kNS + v) * n + q, g);
       }
     }
-    if (ens) {
-      // enstrophy density rho |curl v|^2 / 2 at this Gauss point
-      const double* u = sU + es * kNS * n + q;
-      double ir = 1.0 / u[0];
-      double vv[3] = {u[n] * ir, u[2 * n] * ir, u[3 * n] * ir};
-      double G[3][3];
+    if constexpr (std::is_same<T, double>::value) {
+      if (ens) {
+        // enstrophy density rho |curl v|^2 / 2 at this Gauss point
+        const double* u = sU + es * kNS * n + q;
+        double ir = 1.0 / u[0];
+        double vv[3] = {u[n] * ir, u[2 * n] * ir, u[3 * n] * ir};
+        double G[3][3];
 #pragma unroll
-      for (int j = 0; j < 3; ++j)
+        for (int j = 0; j < 3; ++j)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) G[i][j] = (grad[j * kNS + 1 + i] - grad[j * kNS] * vv[i]) * ir;
-      double wx = G[2][1] - G[1][2], wy = G[0][2] - G[2][0], wz = G[1][0] - G[0][1];
-      double w3 = ops.w[c[0]] * ops.w[c[1]] * ops.w[c[2]];
-      sE[es * n + q] = ops.J * w3 * 0.5 * u[0] * (wx * wx + wy * wy + wz * wz);
+          for (int i = 0; i < 3; ++i) G[i][j] = (grad[j * kNS + 1 + i] - grad[j * kNS] * vv[i]) * ir;
+        double wx = G[2][1] - G[1][2], wy = G[0][2] - G[2][0], wz = G[1][0] - G[0][1];
+        double w3 = ops.w[c[0]] * ops.w[c[1]] * ops.w[c[2]];
+        sE[es * n + q] = ops.J * w3 * 0.5 * u[0] * (wx * wx + wy * wy + wz * wz);
+      }
     }
   }
   __syncthreads();
-  if (ens && threadIdx.x < ne) {  // fixed-order per-element sum (deterministic)
-    double acc = 0.0;
-    for (int k = 0; k < n; ++k) acc += sE[threadIdx.x * n + k];
-    ens[e0 + threadIdx.x] = acc;
+  if constexpr (std::is_same<T, double>::value) {
+    if (ens && threadIdx.x < ne) {  // fixed-order per-element sum (deterministic)
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) acc += sE[threadIdx.x * n + k];
+      ens[e0 + threadIdx.x] = acc;
+    }
   }
-  __syncthreads();
   // minus-face traces of Q: Tq[e][l][c][t] = sum_qn lm[qn] Q[e][c][pt(l,qn,t)]
-  for (int i = threadIdx.x; i < ne * 3 * kNQ * nf; i += T) {
+  for (int i = threadIdx.x; i < ne * 3 * kNQ * nf; i += NT) {
     int es2 = i / (3 * kNQ * nf);
     int r = i - es2 * 3 * kNQ * nf;
     int l = r / (kNQ * nf);
     int r2 = r - l * kNQ * nf;
     int cc = r2 / nf, t = r2 - cc * nf;
     const int st = stride_of<N>(l);
-    const double* row = sQ + (es2 * kNQ + cc) * n + face_point<N>(l, 0, t);
-    double acc = 0.0;
+    const T* row = sQ + (es2 * kNQ + cc) * n + face_point<N>(l, 0, t);
+    T acc{};
 #pragma unroll
-    for (int qn = 0; qn < N; ++qn) acc = fma(ops.lm[qn], row[qn * st], acc);
-    Tq[(e0 + es2) * 3 * kNQ * nf + r] = acc;
+    for (int qn = 0; qn < N; ++qn) acc = fma(o.lm[qn], row[qn * st], acc);
+    R::st(Tq + (e0 + es2) * 3 * kNQ * nf + r, acc);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Kinetic energy of a state held in shared memory (sU: EPC*5*n Gauss
+// Kinetic energy of an FP64 state held in shared memory (sU: EPC*5*n Gauss
 // values; scr: EPC*8*n scratch).  Per element: diag[2e] = computeKE exactly
 // as the reference evaluates it (nodal values weighted by the Gauss weights,
 // solver.cpp:1021-1024, nodal values recovered with Bi (x) Bi (x) Bi), and
@@ -305,17 +327,21 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_ke(const double* __restrict__ U, 
 //       - sum_f (1/alpha_l(f)) L_{s(f)} (x) (Fc*_f + Fv*_f)
 // Fc* is the Roe flux from this element's side; Fv* = -s Fv_l(u_K, q_win)
 // with q from the element on the plus side of the face (numericalFluxV).
+// The RK combination is FP64 on both paths.
+template <class T>
 struct StageArgs {
-  const double* Us;   // stage input state
-  const double* Q;    // its gradient
-  const double* Tu;   // its face traces
-  const double* Tq;   // gradient minus-face traces
+  using S = typename Real<T>::S;
+  const S* Us;        // stage input state
+  const S* Q;         // its gradient
+  const S* Tu;        // its face traces
+  const S* Tq;        // gradient minus-face traces
   const double* Un;   // state at the start of the step
   double* Uacc;       // RK accumulator (u += dt b_s k_s)
-  double* Unext;      // next stage input (u + dt a_s k_s)
-  double* Tu_out;     // traces of Unext (or of Uacc on the last stage)
+  S* Unext;           // next stage input (u + dt a_s k_s); on the last stage
+                      // the mixed path's pair copy of the new state
+  S* Tu_out;          // traces of Unext (or of Uacc on the last stage)
   double* Kout;       // raw RHS output (rhs-only mode)
-  double* diag;       // per-element [ke_ref, ke] on the last stage
+  double* diag;       // per-element [ke_ref, ke] on the last stage (FP64 path)
   int* flag;          // nonzero if a non-finite value was produced
   double cacc;        // dt * b_s
   double cnext;       // dt * a_s
@@ -324,41 +350,44 @@ struct StageArgs {
 
 // Numerical flux sum Fc* + Fv* at face point t of face f (direction L) of
 // element e, written to out[v*nf].
-template <int N, int L>
-__device__ __forceinline__ void face_flux(const StageArgs& a, const DevOps& ops, long e, int f, int t,
-                                          double* out) {
+template <int N, int L, class T>
+__device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& ops, const OpsT<T>& o, long e,
+                                          int f, int t, T* out) {
   constexpr int nf = Cfg<N>::nf;
+  using R = Real<T>;
   const bool plus = f & 1;
-  const double s = plus ? 1.0 : -1.0;
   const long en = face_neighbour((int)e, f, ops.nx, ops.ny, ops.nz);
-  double uK[kNS], uN[kNS], Du[kNQ];
-  const double* tK = a.Tu + (e * 6 + f) * kNS * nf + t;
-  const double* tN = a.Tu + (en * 6 + (f ^ 1)) * kNS * nf + t;
+  T uK[kNS], uN[kNS], Du[kNQ];
+  const auto* tK = a.Tu + (e * 6 + f) * kNS * nf + t;
+  const auto* tN = a.Tu + (en * 6 + (f ^ 1)) * kNS * nf + t;
 #pragma unroll
   for (int v = 0; v < kNS; ++v) {
-    uK[v] = tK[v * nf];
-    uN[v] = tN[v * nf];
+    uK[v] = R::ld(tK + v * nf);
+    uN[v] = R::ld(tN + v * nf);
   }
   // q from the element on the plus side (numericalFluxV kWins switch)
-  const double* tq = a.Tq + ((plus ? en : e) * 3 + L) * kNQ * nf + t;
+  const auto* tq = a.Tq + ((plus ? en : e) * 3 + L) * kNQ * nf + t;
 #pragma unroll
-  for (int k = 0; k < kNQ; ++k) Du[k] = tq[k * nf];
-  double Fc[kNS], Fv[kNS];
-  roe_flux<L>(uN, uK, s, ops.g1, Fc);
-  ViscPre P;
+  for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(tq + k * nf);
+  T Fc[kNS], Fv[kNS];
+  roe_flux<L>(uN, uK, plus, o, Fc);
+  ViscPre<T> P;
   visc_pre(uK, Du, P);
-  visc_column<L>(P, ops.inv_re, ops.kappa, Fv);
+  visc_column<L>(P, o, Fv);
 #pragma unroll
-  for (int v = 0; v < kNS; ++v) out[v * nf] = Fc[v] - s * Fv[v];
+  for (int v = 0; v < kNS; ++v) out[v * nf] = Fc[v] - sgn(plus, Fv[v]);
 }
 
-template <int N>
-__global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ StageArgs a, const __grid_constant__ DevOps ops) {
-  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, EPC = Cfg<N>::EPC, T = Cfg<N>::T;
-  extern __shared__ double smem[];
-  double* sF = smem;                        // EPC*15*n   volume flux Fc - Fv
-  double* sFs = sF + EPC * kNQ * n;         // EPC*6*5*nf face flux sums
-  double* sU = sF;                          // EPC*5*n, aliases sF after use
+template <int N, class T>
+__global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ StageArgs<T> a,
+                                                   const __grid_constant__ DevOps ops,
+                                                   const __grid_constant__ OpsT<T> o) {
+  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, EPC = Cfg<N>::EPC, NT = Cfg<N>::T;
+  using R = Real<T>;
+  extern __shared__ double smem_raw[];
+  T* sF = reinterpret_cast<T*>(smem_raw);  // EPC*15*n   volume flux Fc - Fv
+  T* sFs = sF + EPC * kNQ * n;             // EPC*6*5*nf face flux sums
+  T* sU = sF;                              // EPC*5*n, aliases sF after use
   const int nE = ops.nE;
   const long e0 = (long)blockIdx.x * EPC;
   const int ne = (int)min((long)EPC, nE - e0);
@@ -368,91 +397,88 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ Stage
   // 1. volume fluxes at this Gauss point
   if (act) {
     const long e = e0 + es;
-    double u[kNS], Du[kNQ];
+    T u[kNS], Du[kNQ];
 #pragma unroll
-    for (int v = 0; v < kNS; ++v) u[v] = a.Us[(e * kNS + v) * n + q];
+    for (int v = 0; v < kNS; ++v) u[v] = R::ld(a.Us + (e * kNS + v) * n + q);
 #pragma unroll
-    for (int k = 0; k < kNQ; ++k) Du[k] = a.Q[(e * kNQ + k) * n + q];
-    Euler es_ = euler_state(u, ops.g1, ops.gamma);
-    ViscPre P;
+    for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(a.Q + (e * kNQ + k) * n + q);
+    Euler<T> es_ = euler_state(u, o);
+    ViscPre<T> P;
     visc_pre(u, Du, P);
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
-      double Fc[kNS], Fv[kNS];
+      T Fc[kNS], Fv[kNS];
       euler_column(u, es_, l, Fc);
-      if (l == 0) visc_column<0>(P, ops.inv_re, ops.kappa, Fv);
-      else if (l == 1) visc_column<1>(P, ops.inv_re, ops.kappa, Fv);
-      else visc_column<2>(P, ops.inv_re, ops.kappa, Fv);
+      if (l == 0) visc_column<0>(P, o, Fv);
+      else if (l == 1) visc_column<1>(P, o, Fv);
+      else visc_column<2>(P, o, Fv);
 #pragma unroll
       for (int v = 0; v < kNS; ++v) sF[(es * kNQ + l * kNS + v) * n + q] = Fc[v] - Fv[v];
     }
   }
   // 2. numerical fluxes at the face points
-  for (int i = threadIdx.x; i < ne * 6 * nf; i += T) {
+  for (int i = threadIdx.x; i < ne * 6 * nf; i += NT) {
     const int fes = i / (6 * nf);
     const int r = i - fes * 6 * nf;
     const int f = r / nf, t = r - f * nf;
-    double* out = sFs + (fes * 6 + f) * kNS * nf + t;
+    T* out = sFs + (fes * 6 + f) * kNS * nf + t;
     switch (f >> 1) {
-      case 0: face_flux<N, 0>(a, ops, e0 + fes, f, t, out); break;
-      case 1: face_flux<N, 1>(a, ops, e0 + fes, f, t, out); break;
-      default: face_flux<N, 2>(a, ops, e0 + fes, f, t, out); break;
+      case 0: face_flux<N, 0>(a, ops, o, e0 + fes, f, t, out); break;
+      case 1: face_flux<N, 1>(a, ops, o, e0 + fes, f, t, out); break;
+      default: face_flux<N, 2>(a, ops, o, e0 + fes, f, t, out); break;
     }
   }
   __syncthreads();
   // 3. contraction: K at this Gauss point
-  double K[kNS];
+  T K[kNS];
   if (act) {
 #pragma unroll
-    for (int v = 0; v < kNS; ++v) K[v] = 0.0;
+    for (int v = 0; v < kNS; ++v) K[v] = T{};
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
       const int qn = c[l];
       const int st = stride_of<N>(l);
       const int b = q - qn * st;
       const int t = tangential<N>(l, c[0], c[1], c[2]);
-      const double ia = ops.ia[l];
-      double row[N];
+      const T ia = o.ia[l];
+      T row[N];
 #pragma unroll
-      for (int r = 0; r < N; ++r) row[r] = ops.A[qn * N + r] * ia;
-      const double lp = ops.Lp[qn] * ia, lm = ops.Lm[qn] * ia;
+      for (int r = 0; r < N; ++r) row[r] = o.A[qn * N + r] * ia;
+      const T lp = -(o.Lp[qn] * ia), lm = -(o.Lm[qn] * ia);
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
-        const double* line = sF + (es * kNQ + l * kNS + v) * n + b;
-        double acc = K[v];
+        const T* line = sF + (es * kNQ + l * kNS + v) * n + b;
+        T acc = K[v];
 #pragma unroll
         for (int r = 0; r < N; ++r) acc = fma(row[r], line[r * st], acc);
-        acc = fma(-lm, sFs[((es * 6 + 2 * l) * kNS + v) * nf + t], acc);
-        acc = fma(-lp, sFs[((es * 6 + 2 * l + 1) * kNS + v) * nf + t], acc);
+        acc = fma(lm, sFs[((es * 6 + 2 * l) * kNS + v) * nf + t], acc);
+        acc = fma(lp, sFs[((es * 6 + 2 * l + 1) * kNS + v) * nf + t], acc);
         K[v] = acc;
       }
     }
   }
   __syncthreads();  // sF is reused as sU below
-  // 4. RK4 stage update (or raw RHS output)
+  // 4. RK4 stage update in FP64 (or raw RHS output)
   if (act) {
     const long e = e0 + es;
     if (a.stage < 0) {
 #pragma unroll
-      for (int v = 0; v < kNS; ++v) a.Kout[(e * kNS + v) * n + q] = K[v];
+      for (int v = 0; v < kNS; ++v) a.Kout[(e * kNS + v) * n + q] = R::to_f64(K[v]);
     } else {
       bool bad = false;
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
         const long idx = (e * kNS + v) * n + q;
+        const double kd = R::to_f64(K[v]);
         const double un = a.Un[idx];
         const double acc0 = a.stage == 0 ? un : a.Uacc[idx];
-        const double uacc = acc0 + a.cacc * K[v];
+        const double uacc = acc0 + a.cacc * kd;
         a.Uacc[idx] = uacc;
-        double nxt;
-        if (a.stage < 3) {
-          nxt = un + a.cnext * K[v];
-          a.Unext[idx] = nxt;
-        } else {
-          nxt = uacc;
-        }
+        const double nxt = a.stage < 3 ? un + a.cnext * kd : uacc;
+        const T nt = R::from_f64(nxt);
+        if (a.Unext) R::st(a.Unext + idx, nt);
         bad |= not_finite(nxt);
-        sU[(es * kNS + v) * n + q] = nxt;
+        sU[(es * kNS + v) * n + q] = nt;
       }
       if (bad && a.flag) atomicOr(a.flag, 1);
     }
@@ -460,11 +486,14 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ Stage
   if (a.stage < 0) return;
   __syncthreads();
   // 5. traces of the next stage input for the face fluxes of the next pass
-  write_traces<N>(sU, ne, e0, a.Tu_out, ops);
-  // 6. diagnostics on the new state (last stage only)
-  if (a.stage == 3 && a.diag) {
-    __syncthreads();
-    ke_tail<N>(sU, sF + EPC * kNS * n, ne, e0, a.diag, ops);
+  write_traces<N, T>(sU, ne, e0, a.Tu_out, o);
+  // 6. diagnostics on the new state (last stage of the FP64 path; the mixed
+  //    path runs k_ke on the FP64 state instead)
+  if constexpr (std::is_same<T, double>::value) {
+    if (a.stage == 3 && a.diag) {
+      __syncthreads();
+      ke_tail<N>(sU, sF + EPC * kNS * n, ne, e0, a.diag, ops);
+    }
   }
 }
 

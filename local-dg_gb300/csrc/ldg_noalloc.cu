@@ -65,7 +65,8 @@ cudaError_t scratch_address(int device, double** out) {
 }
 
 template <int N>
-cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& ops, cudaStream_t st) {
+cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& ops, const OpsT<double>& o,
+                    cudaStream_t st) {
   using C = Cfg<N>;
   const int nE = ops.nE;
   const size_t ne = (size_t)nE;
@@ -79,15 +80,15 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   const size_t sm_r = sizeof(double) * C::EPC * (kNQ * C::n + 6 * kNS * C::nf);
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(k_transform<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tr)) ||
-      (e = cudaFuncSetAttribute(k_traces<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_trc)) ||
-      (e = cudaFuncSetAttribute(k_grad<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_g)) ||
-      (e = cudaFuncSetAttribute(k_rhs<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_r)))
+      (e = cudaFuncSetAttribute(k_traces<N, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_trc)) ||
+      (e = cudaFuncSetAttribute(k_grad<N, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_g)) ||
+      (e = cudaFuncSetAttribute(k_rhs<N, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_r)))
     return e;
   const int grid = (nE + C::EPC - 1) / C::EPC;
   k_transform<N><<<grid, C::T, sm_tr, st>>>(u, U, nE, kNS, ops, 0);
-  k_traces<N><<<grid, C::T, sm_trc, st>>>(U, Tu, nE, ops);
-  k_grad<N><<<grid, C::T, sm_g, st>>>(U, Tu, Q, Tq, nullptr, ops);
-  StageArgs a;
+  k_traces<N, double><<<grid, C::T, sm_trc, st>>>(U, nullptr, Tu, nE, o);
+  k_grad<N, double><<<grid, C::T, sm_g, st>>>(U, Tu, Q, Tq, nullptr, ops, o);
+  StageArgs<double> a;
   std::memset(&a, 0, sizeof(a));
   a.Us = U;
   a.Q = Q;
@@ -95,7 +96,7 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   a.Tq = Tq;
   a.Kout = U;  // each thread overwrites only the Gauss point it alone read
   a.stage = -1;
-  k_rhs<N><<<grid, C::T, sm_r, st>>>(a, ops);
+  k_rhs<N, double><<<grid, C::T, sm_r, st>>>(a, ops, o);
   k_transform<N><<<grid, C::T, sm_tr, st>>>(U, k, nE, kNS, ops, 1);
   return cudaGetLastError();
 }
@@ -160,6 +161,7 @@ extern "C" int ldg_rhs_noalloc(const ldg_config* cfg, const double* u, double* k
   ops.ny = c.ny;
   ops.nz = c.nz;
   ops.nE = (int)nE;
+  const OpsT<double> o = make_opst<double>(ops, N);
 
   int prev = 0;
   if (cudaGetDevice(&prev) != cudaSuccess) {
@@ -173,12 +175,12 @@ extern "C" int ldg_rhs_noalloc(const ldg_config* cfg, const double* u, double* k
   if (e == cudaSuccess) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     switch (N) {
-      case 2: e = run_rhs<2>(u, k, scratch, ops, st); break;
-      case 3: e = run_rhs<3>(u, k, scratch, ops, st); break;
-      case 4: e = run_rhs<4>(u, k, scratch, ops, st); break;
-      case 5: e = run_rhs<5>(u, k, scratch, ops, st); break;
-      case 6: e = run_rhs<6>(u, k, scratch, ops, st); break;
-      default: e = run_rhs<7>(u, k, scratch, ops, st); break;
+      case 2: e = run_rhs<2>(u, k, scratch, ops, o, st); break;
+      case 3: e = run_rhs<3>(u, k, scratch, ops, o, st); break;
+      case 4: e = run_rhs<4>(u, k, scratch, ops, o, st); break;
+      case 5: e = run_rhs<5>(u, k, scratch, ops, o, st); break;
+      case 6: e = run_rhs<6>(u, k, scratch, ops, o, st); break;
+      default: e = run_rhs<7>(u, k, scratch, ops, o, st); break;
     }
   }
   if (prev != c.device) cudaSetDevice(prev);

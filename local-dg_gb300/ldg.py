@@ -37,6 +37,8 @@ LDG_OK = 0
 LDG_HOST = 0
 LDG_DEVICE = 1
 LDG_FP64 = 0
+LDG_MIXED_F32X2 = 1
+PRECISIONS = {"fp64": LDG_FP64, "mixed": LDG_MIXED_F32X2}
 
 
 def _nvcc() -> str:
@@ -200,7 +202,7 @@ class Solver:
     def __init__(self, p: int, nx: int, ny: int | None = None, nz: int | None = None, *, L: float = 1.0,
                  tf: float | None = None, steps: int | None = None, Re: float = 1600.0, Pr: float = 0.71,
                  gamma: float = 1.4, Ma: float = 0.1, cfl: float = 0.01, device: int = 0,
-                 check_finite: bool = True, dt_snaps: int = 0, box=None):
+                 check_finite: bool = True, dt_snaps: int = 0, box=None, precision: str = "fp64"):
         L_ = load()
         cfg = LdgConfig()
         _check(L_.ldg_config_default(ctypes.byref(cfg)), "ldg_config_default")
@@ -213,6 +215,7 @@ class Solver:
         cfg.tf = tf
         cfg.Re, cfg.Pr, cfg.gamma, cfg.Ma, cfg.cfl = Re, Pr, gamma, Ma, cfl
         cfg.device = device
+        cfg.precision = PRECISIONS[precision]
         cfg.check_finite = 1 if check_finite else 0
         cfg.dt_snaps = dt_snaps
         if box is not None:
