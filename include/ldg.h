@@ -46,6 +46,7 @@ extern "C" {
 #define LDG_ERR_NONFINITE -4   /* NaN/Inf found in the state after a step  */
 #define LDG_ERR_UNSUPPORTED -5 /* order or mode not built                  */
 #define LDG_ERR_NODEVICE -6    /* no CUDA device visible                   */
+#define LDG_ERR_TIMEOUT -7     /* a bounded on-device wait gave up          */
 
 /* where a pointer lives */
 #define LDG_HOST 0
@@ -76,7 +77,15 @@ typedef struct ldg_config {
                        1: [box_lo, box_hi] (Mesh botLeft/topRight,
                        mesh.cpp:51-151); periodic either way             */
   double box_lo[3], box_hi[3];
-  int reserved[8];
+  /* Seeded velocity perturbation added to the Taylor-Green initial
+   * condition (no reference counterpart; ensemble inputs):
+   *   dv_c = perturb_amp*V0/12 * sum_{k=1..4} sum_{d=x,y,z} sin(k x_d/L + phi)
+   * with phases phi = 2 pi U[0,1) from SplitMix64 keyed by (seed, instance,
+   * c, k, d).  perturb_amp = 0 gives the reference's initial condition. */
+  double perturb_amp;
+  unsigned long long seed;
+  int instance;
+  int reserved[7];
 } ldg_config;
 
 typedef struct ldg_info {
@@ -166,6 +175,31 @@ int ldg_kernel_times(ldg_solver* s, double* ms, long long* launches, int max_cla
  * a register-resident FMA chain; the roofline denominator for the FP64
  * kernels.  (No reference counterpart.) */
 int ldg_probe_fp64_peak(int device, double* tflops);
+
+/* ---- Batched ensemble.  No reference counterpart (the reference runs one
+ * problem per MPI job).  Members are independent problems, each an
+ * ldg_config (p in 2..4, LDG_FP64, all on one device; mesh size, order, Re
+ * and the seeded perturbation may differ).  Every RK4 stage of all members
+ * is one persistent kernel launch over a work queue of (member, element
+ * block) items; a step (4 launches + KE reductions) is replayed from a CUDA
+ * graph.  Each member's state and KE series equal a solo ldg_create/ldg_step
+ * run of the same config bit for bit.  The tile shape (threads per CTA) and
+ * the persistent grid size are picked by timing at creation. */
+typedef struct ldg_ensemble ldg_ensemble;
+int ldg_ensemble_create(const ldg_config* cfgs, int count, ldg_ensemble** out);
+int ldg_ensemble_destroy(ldg_ensemble* e);
+/* nsteps RK4 steps of every member (each with its own dt). */
+int ldg_ensemble_step(ldg_ensemble* e, int nsteps);
+/* A member's state in the reference layout (host or device pointer). */
+int ldg_ensemble_get_state(ldg_ensemble* e, int member, double* u, int where);
+/* A member's computeKE series, one entry per step. */
+int ldg_ensemble_ke_history(ldg_ensemble* e, int member, double* ke, int max, int* count);
+int ldg_ensemble_member_info(const ldg_ensemble* e, int member, ldg_info* info);
+/* The autotuner's choice and its timings: stage_ms[tile*4 + g] for tiles
+ * {128, 256 threads} x grids {1, 2, 4, 8} x SM count. */
+int ldg_ensemble_tuning(const ldg_ensemble* e, int* threads_per_cta, int* persistent_ctas, float* stage_ms,
+                        int max);
+void* ldg_ensemble_stream(ldg_ensemble* e);
 
 /* RHS evaluation without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot let the library allocate

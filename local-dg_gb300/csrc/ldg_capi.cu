@@ -13,6 +13,7 @@
 #include "../../include/ldg.h"
 #include "ldg_kernels.cuh"
 #include "ldg_ops.hpp"
+#include "ldg_problem.hpp"
 
 using namespace ldg;
 
@@ -84,6 +85,8 @@ struct IcArgs {
   double xi[kMaxN];
   double lo[3], hi[3];
   double p0, rho0, V0, R, T0, gamma, L;
+  double amp;            // perturbation amplitude * V0 / 12 (0: none)
+  double phi[3][4][3];   // phases [component][wavenumber-1][direction]
   int N, nx, ny, nz;
 };
 
@@ -107,12 +110,42 @@ __global__ void k_taylor_green(double* __restrict__ u, long total, const __grid_
   double mx = a.rho0 * a.V0 * sin(x / L) * cos(y / L) * cos(z / L);
   double my = -a.rho0 * a.V0 * cos(x / L) * sin(y / L) * cos(z / L);
   double mz = 0 * a.rho0;
+  if (a.amp != 0.0) {
+    const double X[3] = {x / L, y / L, z / L};
+    double dv[3] = {0, 0, 0};
+    for (int cpt = 0; cpt < 3; ++cpt)
+      for (int k = 1; k <= 4; ++k)
+        for (int d = 0; d < 3; ++d) dv[cpt] += sin(k * X[d] + a.phi[cpt][k - 1][d]);
+    mx += a.rho0 * a.amp * dv[0];
+    my += a.rho0 * a.amp * dv[1];
+    mz += a.rho0 * a.amp * dv[2];
+  }
   double* uk = u + k * 5 * n;
   uk[v] = r;
   uk[v + n] = mx;
   uk[v + 2 * n] = my;
   uk[v + 3 * n] = mz;
   uk[v + 4 * n] = pr / (a.gamma - 1) + (mx * mx + my * my + mz * mz) / (2.0 * r);
+}
+
+// SplitMix64 (Steele, Lea & Flood, OOPSLA 2014): counter-based stream.
+unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// Phases of the seeded velocity perturbation, 2 pi U[0,1) per
+// (component, wavenumber, direction).
+void perturbation_phases(unsigned long long seed, int instance, double phi[3][4][3]) {
+  const unsigned long long base = splitmix64(seed ^ splitmix64(0x4C44470000000000ULL + (unsigned)instance));
+  for (int c = 0; c < 3; ++c)
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) {
+        unsigned long long r = splitmix64(base + (unsigned long long)(c * 16 + k * 4 + d));
+        phi[c][k][d] = 2.0 * M_PI * (double)(r >> 11) * (1.0 / 9007199254740992.0);
+      }
 }
 
 // Deterministic single-CTA sum: out[0] = scale * sum_i x[i*stride + off].
@@ -409,6 +442,131 @@ int ensure_ke_capacity(ldg_solver* s, long long need) {
 
 }  // namespace
 
+namespace ldg {
+
+int setup_problem(const ldg_config& c, Problem* pb, std::string* err) {
+  if (c.p < 1 || c.p > 6) return *err = "order p must be 1..6", LDG_ERR_UNSUPPORTED;
+  if (c.nx < 3 || c.ny < 3 || c.nz < 3)  // mesh.cpp:102-107
+    return *err = "each direction needs at least 3 elements", LDG_ERR_INVALID;
+  if (!(c.tf > 0) || !(c.Re > 0) || !(c.Pr > 0) || !(c.gamma > 1) || !(c.Ma > 0) || !(c.cfl > 0) || !(c.L > 0))
+    return *err = "physical parameters must be positive (gamma > 1)", LDG_ERR_INVALID;
+  if (c.precision != LDG_FP64 && c.precision != LDG_MIXED_F32X2)
+    return *err = "precision mode not built", LDG_ERR_UNSUPPORTED;
+  if ((long long)c.nx * c.ny * c.nz > 0x7fffffffLL / 8) return *err = "mesh too large", LDG_ERR_INVALID;
+  if (!(c.perturb_amp >= 0)) return *err = "perturbation amplitude must be >= 0", LDG_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return *err = "no CUDA device", LDG_ERR_NODEVICE;
+  }
+  if (c.device < 0 || c.device >= ndev) return *err = "bad device ordinal", LDG_ERR_INVALID;
+  pb->cfg = c;
+  pb->N = c.p + 1;
+  pb->n = pb->N * pb->N * pb->N;
+  pb->nf = pb->N * pb->N;
+  pb->nE = c.nx * c.ny * c.nz;
+  if (!build_ops1d(c.p, &pb->o1)) return *err = "operator setup failed", LDG_ERR_UNSUPPORTED;
+  // Domain (driver.cpp:28-31 / Mesh botLeft, topRight) and element sizes
+  // (mesh.cpp:149-151).
+  double size = M_PI * c.L;
+  for (int l = 0; l < 3; ++l) {
+    pb->lo[l] = c.use_box ? c.box_lo[l] : -size;
+    pb->hi[l] = c.use_box ? c.box_hi[l] : size;
+  }
+  const int nd[3] = {c.nx, c.ny, c.nz};
+  double mind[3];
+  for (int l = 0; l < 3; ++l) {
+    mind[l] = (pb->hi[l] - pb->lo[l]) / nd[l];
+    if (!(mind[l] > 0)) return *err = "empty box", LDG_ERR_INVALID;
+  }
+  // Physics and time step (solver.cpp:30-52).
+  const double c0 = pb->V0 / c.Ma;
+  pb->p0 = pb->rho0 * c0 * c0 / c.gamma;
+  pb->T0 = pb->p0 / (pb->R * pb->rho0);
+  const double maxVel = pb->V0;
+  pb->dt = c.cfl * std::min(std::min(mind[0], mind[1]), mind[2]) / (maxVel * (2 * c.p + 1));
+  pb->tf = c.tf;
+  pb->timesteps = (long long)std::ceil(c.tf / pb->dt);
+  if (pb->timesteps < 1) pb->timesteps = 1;
+  pb->dt = c.tf / pb->timesteps;
+  for (int i = 0; i < kMaxN; ++i) pb->xi[i] = 0.0;
+  for (int i = 0; i <= c.p; ++i) pb->xi[i] = std::cos((c.p - i) * M_PI / c.p);  // dgMath.cpp:41
+  // Device operator block.
+  DevOps& o = pb->ops;
+  std::memset(&o, 0, sizeof(o));
+  const int N = pb->N;
+  for (int i = 0; i < N * N; ++i) {
+    o.A[i] = pb->o1.A[i];
+    o.B[i] = pb->o1.B[i];
+    o.Bi[i] = pb->o1.Bi[i];
+  }
+  for (int i = 0; i < N; ++i) {
+    o.lp[i] = pb->o1.lp[i];
+    o.lm[i] = pb->o1.lm[i];
+    o.Lp[i] = pb->o1.Lp[i];
+    o.Lm[i] = pb->o1.Lm[i];
+    o.w[i] = pb->o1.w[i];
+  }
+  double alpha[3];
+  for (int l = 0; l < 3; ++l) {
+    alpha[l] = mind[l] / 2.0;  // solver.cpp:144-148
+    o.ia[l] = 1.0 / alpha[l];
+  }
+  o.J = alpha[0] * alpha[1] * alpha[2];
+  o.inv_re = 1.0 / c.Re;
+  o.gamma = c.gamma;
+  o.g1 = (c.gamma == 1.4) ? 0.4 : c.gamma - 1.0;  // the reference's literal 0.4
+  o.kappa = c.gamma * (1.0 / c.Pr);
+  o.ke_norm = 1.0 / (pb->rho0 * std::pow(2 * M_PI * c.L, 3.0));  // solver.cpp:1031
+  o.nx = c.nx;
+  o.ny = c.ny;
+  o.nz = c.nz;
+  o.nE = pb->nE;
+  return LDG_OK;
+}
+
+cudaError_t launch_initial_condition(const Problem& pb, double* nodal, cudaStream_t st) {
+  IcArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.amp = pb.cfg.perturb_amp * pb.V0 / 12.0;
+  perturbation_phases(pb.cfg.seed, pb.cfg.instance, a.phi);
+  for (int i = 0; i < pb.N; ++i) a.xi[i] = pb.xi[i];
+  for (int l = 0; l < 3; ++l) {
+    a.lo[l] = pb.lo[l];
+    a.hi[l] = pb.hi[l];
+  }
+  a.p0 = pb.p0;
+  a.rho0 = pb.rho0;
+  a.V0 = pb.V0;
+  a.R = pb.R;
+  a.T0 = pb.T0;
+  a.gamma = pb.cfg.gamma;
+  a.L = pb.cfg.L;
+  a.N = pb.N;
+  a.nx = pb.cfg.nx;
+  a.ny = pb.cfg.ny;
+  a.nz = pb.cfg.nz;
+  const long total = (long)pb.nE * pb.n;
+  k_taylor_green<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(nodal, total, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transform_any(int N, const double* in, double* out, int nE, const DevOps& ops, int inverse,
+                                 cudaStream_t st) {
+  cudaError_t e = d_attrs(N);
+  if (e != cudaSuccess) return e;
+  return d_transform(N, in, out, nE, ops, inverse, st);
+}
+
+cudaError_t launch_traces_fp64(int N, const double* U, double* Tu, int nE, const OpsT<double>& o,
+                               cudaStream_t st) {
+  cudaError_t e = d_attrs(N);
+  if (e != cudaSuccess) return e;
+  LDG_DISPATCH(N, (launch_traces<NN, double>(U, nullptr, Tu, nE, o, st)));
+}
+
+}  // namespace ldg
+
 extern "C" {
 
 int ldg_abi_version(void) { return LDG_ABI_VERSION; }
@@ -422,6 +580,7 @@ const char* ldg_error_string(int status) {
     case LDG_ERR_NONFINITE: return "LDG_ERR_NONFINITE";
     case LDG_ERR_UNSUPPORTED: return "LDG_ERR_UNSUPPORTED";
     case LDG_ERR_NODEVICE: return "LDG_ERR_NODEVICE";
+    case LDG_ERR_TIMEOUT: return "LDG_ERR_TIMEOUT";
   }
   return "LDG_ERR_UNKNOWN";
 }
@@ -452,91 +611,32 @@ int ldg_create(const ldg_config* cfg, ldg_solver** out) {
   if (!cfg || !out) return fail(LDG_ERR_INVALID, "null argument");
   *out = nullptr;
   const ldg_config& c = *cfg;
-  if (c.p < 1 || c.p > 6) return fail(LDG_ERR_UNSUPPORTED, "order p must be 1..6");
-  if (c.nx < 3 || c.ny < 3 || c.nz < 3)  // mesh.cpp:102-107
-    return fail(LDG_ERR_INVALID, "each direction needs at least 3 elements");
-  if (!(c.tf > 0) || !(c.Re > 0) || !(c.Pr > 0) || !(c.gamma > 1) || !(c.Ma > 0) || !(c.cfl > 0) || !(c.L > 0))
-    return fail(LDG_ERR_INVALID, "physical parameters must be positive (gamma > 1)");
-  if (c.precision != LDG_FP64 && c.precision != LDG_MIXED_F32X2)
-    return fail(LDG_ERR_UNSUPPORTED, "precision mode not built");
-  if ((long long)c.nx * c.ny * c.nz > 0x7fffffffLL / 8) return fail(LDG_ERR_INVALID, "mesh too large");
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-    cudaGetLastError();
-    return fail(LDG_ERR_NODEVICE, "no CUDA device");
-  }
-  if (c.device < 0 || c.device >= ndev) return fail(LDG_ERR_INVALID, "bad device ordinal");
+  Problem pb;
+  std::string err;
+  int pst = setup_problem(c, &pb, &err);
+  if (pst != LDG_OK) return fail(pst, err);
   ldg_solver* s = new (std::nothrow) ldg_solver();
   if (!s) return fail(LDG_ERR_NOMEM, "host allocation");
   s->cfg = c;
-  s->N = c.p + 1;
-  s->n = s->N * s->N * s->N;
-  s->nf = s->N * s->N;
-  s->nE = c.nx * c.ny * c.nz;
-  if (!build_ops1d(c.p, &s->o1)) {
-    delete s;
-    return fail(LDG_ERR_UNSUPPORTED, "operator setup failed");
-  }
-  // Domain (driver.cpp:28-31 / Mesh botLeft, topRight) and element sizes
-  // (mesh.cpp:149-151).
-  double size = M_PI * c.L;
+  s->N = pb.N;
+  s->n = pb.n;
+  s->nf = pb.nf;
+  s->nE = pb.nE;
+  s->o1 = pb.o1;
   for (int l = 0; l < 3; ++l) {
-    s->lo[l] = c.use_box ? c.box_lo[l] : -size;
-    s->hi[l] = c.use_box ? c.box_hi[l] : size;
+    s->lo[l] = pb.lo[l];
+    s->hi[l] = pb.hi[l];
   }
-  const int nd[3] = {c.nx, c.ny, c.nz};
-  double mind[3];
-  for (int l = 0; l < 3; ++l) {
-    mind[l] = (s->hi[l] - s->lo[l]) / nd[l];
-    if (!(mind[l] > 0)) {
-      delete s;
-      return fail(LDG_ERR_INVALID, "empty box");
-    }
-  }
-  // Physics and time step (solver.cpp:30-52).
-  const double c0 = s->V0 / c.Ma;
-  s->p0 = s->rho0 * c0 * c0 / c.gamma;
-  s->T0 = s->p0 / (s->R * s->rho0);
-  const double maxVel = s->V0;
-  s->dt = c.cfl * std::min(std::min(mind[0], mind[1]), mind[2]) / (maxVel * (2 * c.p + 1));
-  s->tf = c.tf;
-  s->timesteps = (long long)std::ceil(c.tf / s->dt);
-  if (s->timesteps < 1) s->timesteps = 1;
-  s->dt = c.tf / s->timesteps;
-  for (int i = 0; i <= c.p; ++i) s->xi[i] = std::cos((c.p - i) * M_PI / c.p);  // dgMath.cpp:41
-  // Device operator block.
-  DevOps& o = s->ops;
-  std::memset(&o, 0, sizeof(o));
+  s->p0 = pb.p0;
+  s->T0 = pb.T0;
+  s->dt = pb.dt;
+  s->tf = pb.tf;
+  s->timesteps = pb.timesteps;
+  for (int i = 0; i < kMaxN; ++i) s->xi[i] = pb.xi[i];
+  s->ops = pb.ops;
   const int N = s->N;
-  for (int i = 0; i < N * N; ++i) {
-    o.A[i] = s->o1.A[i];
-    o.B[i] = s->o1.B[i];
-    o.Bi[i] = s->o1.Bi[i];
-  }
-  for (int i = 0; i < N; ++i) {
-    o.lp[i] = s->o1.lp[i];
-    o.lm[i] = s->o1.lm[i];
-    o.Lp[i] = s->o1.Lp[i];
-    o.Lm[i] = s->o1.Lm[i];
-    o.w[i] = s->o1.w[i];
-  }
-  double alpha[3];
-  for (int l = 0; l < 3; ++l) {
-    alpha[l] = mind[l] / 2.0;  // solver.cpp:144-148
-    o.ia[l] = 1.0 / alpha[l];
-  }
-  o.J = alpha[0] * alpha[1] * alpha[2];
-  o.inv_re = 1.0 / c.Re;
-  o.gamma = c.gamma;
-  o.g1 = (c.gamma == 1.4) ? 0.4 : c.gamma - 1.0;  // the reference's literal 0.4
-  o.kappa = c.gamma * (1.0 / c.Pr);
-  o.ke_norm = 1.0 / (s->rho0 * std::pow(2 * M_PI * c.L, 3.0));  // solver.cpp:1031
-  o.nx = c.nx;
-  o.ny = c.ny;
-  o.nz = c.nz;
-  o.nE = s->nE;
-  s->o64 = make_opst<double>(o, N);
-  s->odd = make_opst<dd>(o, N);
+  s->o64 = make_opst<double>(s->ops, N);
+  s->odd = make_opst<dd>(s->ops, N);
   s->mixed = c.precision == LDG_MIXED_F32X2;
 
   int st;
@@ -610,27 +710,20 @@ int ldg_get_info(const ldg_solver* s, ldg_info* info) {
 int ldg_set_initial_condition(ldg_solver* s) {
   if (!s) return fail(LDG_ERR_INVALID, "null solver");
   LDG_CUDA(cudaSetDevice(s->cfg.device));
-  IcArgs a;
-  std::memset(&a, 0, sizeof(a));
-  for (int i = 0; i < s->N; ++i) a.xi[i] = s->xi[i];
+  Problem pb;
+  pb.cfg = s->cfg;
+  pb.N = s->N;
+  pb.n = s->n;
+  pb.nf = s->nf;
+  pb.nE = s->nE;
+  for (int i = 0; i < kMaxN; ++i) pb.xi[i] = s->xi[i];
   for (int l = 0; l < 3; ++l) {
-    a.lo[l] = s->lo[l];
-    a.hi[l] = s->hi[l];
+    pb.lo[l] = s->lo[l];
+    pb.hi[l] = s->hi[l];
   }
-  a.p0 = s->p0;
-  a.rho0 = s->rho0;
-  a.V0 = s->V0;
-  a.R = s->R;
-  a.T0 = s->T0;
-  a.gamma = s->cfg.gamma;
-  a.L = s->cfg.L;
-  a.N = s->N;
-  a.nx = s->cfg.nx;
-  a.ny = s->cfg.ny;
-  a.nz = s->cfg.nz;
-  const long total = (long)s->nE * s->n;
-  k_taylor_green<<<(unsigned)((total + 255) / 256), 256, 0, s->stream>>>(s->nodal, total, a);
-  LDG_CUDA(cudaGetLastError());
+  pb.p0 = s->p0;
+  pb.T0 = s->T0;
+  LDG_CUDA(launch_initial_condition(pb, s->nodal, s->stream));
   s->step = 0;
   return load_state_from_nodal(s);
 }

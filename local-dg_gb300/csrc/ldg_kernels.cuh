@@ -33,11 +33,17 @@
 
 namespace ldg {
 
+// Default elements per CTA ("tile") of the solo kernels.
 template <int N>
+struct DefEPC {
+  static constexpr int value = N == 2 ? 32 : N == 3 ? 9 : N == 4 ? 4 : N == 5 ? 2 : 1;
+};
+
+template <int N, int E = DefEPC<N>::value>
 struct Cfg {
   static constexpr int n = N * N * N;
   static constexpr int nf = N * N;
-  static constexpr int EPC = N == 2 ? 32 : N == 3 ? 9 : N == 4 ? 4 : N == 5 ? 2 : 1;
+  static constexpr int EPC = E;
   static constexpr int T = ((EPC * n + 31) / 32) * 32;
 };
 
@@ -107,10 +113,10 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_transform(const double* __restric
 // ---------------------------------------------------------------------------
 // Face traces of a state held in shared memory:
 // Tu[e][f][v][t] = sum_qn l_{+-}[qn] U[e][v][pt].
-template <int N, class T>
+template <int N, class T, int E = DefEPC<N>::value>
 __device__ __forceinline__ void write_traces(const T* sU, int ne, long e0, typename Real<T>::S* Tu,
                                              const OpsT<T>& o) {
-  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, NT = Cfg<N>::T;
+  constexpr int n = Cfg<N, E>::n, nf = Cfg<N, E>::nf, NT = Cfg<N, E>::T;
   for (int i = threadIdx.x; i < ne * 6 * kNS * nf; i += NT) {
     int es = i / (6 * kNS * nf);
     int r = i - es * 6 * kNS * nf;
@@ -156,25 +162,20 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_traces(const double* __restrict__
 // side of every face, so only plus-face traces are read.
 // Writes Q and the minus-face traces Tq; on the FP64 path optionally the
 // per-element enstrophy.
-template <int N, class T>
-__global__ void __launch_bounds__(Cfg<N>::T) k_grad(const typename Real<T>::S* __restrict__ U,
-                                                    const typename Real<T>::S* __restrict__ Tu,
-                                                    typename Real<T>::S* __restrict__ Q,
-                                                    typename Real<T>::S* __restrict__ Tq,
-                                                    double* __restrict__ ens,
-                                                    const __grid_constant__ DevOps ops,
-                                                    const __grid_constant__ OpsT<T> o) {
-  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, EPC = Cfg<N>::EPC, NT = Cfg<N>::T;
+template <int N, class T, int E = DefEPC<N>::value>
+__device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict__ U,
+                                          const typename Real<T>::S* __restrict__ Tu,
+                                          typename Real<T>::S* __restrict__ Q,
+                                          typename Real<T>::S* __restrict__ Tq, double* __restrict__ ens,
+                                          const DevOps& ops, const OpsT<T>& o, long e0, int ne,
+                                          double* smem_raw) {
+  constexpr int n = Cfg<N, E>::n, nf = Cfg<N, E>::nf, EPC = Cfg<N, E>::EPC, NT = Cfg<N, E>::T;
   using R = Real<T>;
-  extern __shared__ double smem_raw[];
   T* sU = reinterpret_cast<T*>(smem_raw);  // EPC*5*n
   T* sQ = sU + EPC * kNS * n;              // EPC*15*n
   T* sTp = sQ + EPC * kNQ * n;             // EPC*3*5*nf  own +l traces
   T* sTm = sTp + EPC * 3 * kNS * nf;       // EPC*3*5*nf  (-l neighbour)'s +l traces
   double* sE = reinterpret_cast<double*>(sTm + EPC * 3 * kNS * nf);  // EPC*n enstrophy
-  const int nE = ops.nE;
-  const long e0 = (long)blockIdx.x * EPC;
-  const int ne = (int)min((long)EPC, nE - e0);
   for (int i = threadIdx.x; i < ne * kNS * n; i += NT) sU[i] = R::ld(U + e0 * kNS * n + i);
   for (int i = threadIdx.x; i < ne * 3 * kNS * nf; i += NT) {
     int es = i / (3 * kNS * nf);
@@ -256,16 +257,30 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_grad(const typename Real<T>::S* _
   }
 }
 
+template <int N, class T>
+__global__ void __launch_bounds__(Cfg<N>::T) k_grad(const typename Real<T>::S* __restrict__ U,
+                                                    const typename Real<T>::S* __restrict__ Tu,
+                                                    typename Real<T>::S* __restrict__ Q,
+                                                    typename Real<T>::S* __restrict__ Tq,
+                                                    double* __restrict__ ens,
+                                                    const __grid_constant__ DevOps ops,
+                                                    const __grid_constant__ OpsT<T> o) {
+  extern __shared__ double smem_raw[];
+  const long e0 = (long)blockIdx.x * Cfg<N>::EPC;
+  const int ne = (int)min((long)Cfg<N>::EPC, ops.nE - e0);
+  grad_body<N, T>(U, Tu, Q, Tq, ens, ops, o, e0, ne, smem_raw);
+}
+
 // ---------------------------------------------------------------------------
 // Kinetic energy of an FP64 state held in shared memory (sU: EPC*5*n Gauss
 // values; scr: EPC*8*n scratch).  Per element: diag[2e] = computeKE exactly
 // as the reference evaluates it (nodal values weighted by the Gauss weights,
 // solver.cpp:1021-1024, nodal values recovered with Bi (x) Bi (x) Bi), and
 // diag[2e+1] = the Gauss-quadrature kinetic energy.  Fixed-order sums.
-template <int N>
+template <int N, int E = DefEPC<N>::value>
 __device__ __forceinline__ void ke_tail(const double* sU, double* scr, int ne, long e0, double* diag,
                                         const DevOps& ops) {
-  constexpr int n = Cfg<N>::n, EPC = Cfg<N>::EPC;
+  constexpr int n = Cfg<N, E>::n, EPC = Cfg<N, E>::EPC;
   double* s1 = scr;                 // EPC*4*n
   double* s2 = scr + EPC * 4 * n;   // EPC*4*n
   const int es = threadIdx.x / n, q = threadIdx.x % n;
@@ -353,7 +368,7 @@ struct StageArgs {
 template <int N, int L, class T>
 __device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& ops, const OpsT<T>& o, long e,
                                           int f, int t, T* out) {
-  constexpr int nf = Cfg<N>::nf;
+  constexpr int nf = N * N;
   using R = Real<T>;
   const bool plus = f & 1;
   const long en = face_neighbour((int)e, f, ops.nx, ops.ny, ops.nz);
@@ -378,19 +393,14 @@ __device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& o
   for (int v = 0; v < kNS; ++v) out[v * nf] = Fc[v] - sgn(plus, Fv[v]);
 }
 
-template <int N, class T>
-__global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ StageArgs<T> a,
-                                                   const __grid_constant__ DevOps ops,
-                                                   const __grid_constant__ OpsT<T> o) {
-  constexpr int n = Cfg<N>::n, nf = Cfg<N>::nf, EPC = Cfg<N>::EPC, NT = Cfg<N>::T;
+template <int N, class T, int E = DefEPC<N>::value>
+__device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& ops, const OpsT<T>& o, long e0,
+                                         int ne, double* smem_raw) {
+  constexpr int n = Cfg<N, E>::n, nf = Cfg<N, E>::nf, EPC = Cfg<N, E>::EPC, NT = Cfg<N, E>::T;
   using R = Real<T>;
-  extern __shared__ double smem_raw[];
   T* sF = reinterpret_cast<T*>(smem_raw);  // EPC*15*n   volume flux Fc - Fv
   T* sFs = sF + EPC * kNQ * n;             // EPC*6*5*nf face flux sums
   T* sU = sF;                              // EPC*5*n, aliases sF after use
-  const int nE = ops.nE;
-  const long e0 = (long)blockIdx.x * EPC;
-  const int ne = (int)min((long)EPC, nE - e0);
   const int es = threadIdx.x / n, q = threadIdx.x % n;
   const bool act = es < ne;
   const int c[3] = {q % N, (q / N) % N, q / (N * N)};
@@ -486,15 +496,25 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ Stage
   if (a.stage < 0) return;
   __syncthreads();
   // 5. traces of the next stage input for the face fluxes of the next pass
-  write_traces<N, T>(sU, ne, e0, a.Tu_out, o);
+  write_traces<N, T, E>(sU, ne, e0, a.Tu_out, o);
   // 6. diagnostics on the new state (last stage of the FP64 path; the mixed
   //    path runs k_ke on the FP64 state instead)
   if constexpr (std::is_same<T, double>::value) {
     if (a.stage == 3 && a.diag) {
       __syncthreads();
-      ke_tail<N>(sU, sF + EPC * kNS * n, ne, e0, a.diag, ops);
+      ke_tail<N, E>(sU, sF + EPC * kNS * n, ne, e0, a.diag, ops);
     }
   }
+}
+
+template <int N, class T>
+__global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ StageArgs<T> a,
+                                                   const __grid_constant__ DevOps ops,
+                                                   const __grid_constant__ OpsT<T> o) {
+  extern __shared__ double smem_raw[];
+  const long e0 = (long)blockIdx.x * Cfg<N>::EPC;
+  const int ne = (int)min((long)Cfg<N>::EPC, ops.nE - e0);
+  rhs_body<N, T>(a, ops, o, e0, ne, smem_raw);
 }
 
 }  // namespace ldg

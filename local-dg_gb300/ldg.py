@@ -31,7 +31,7 @@ LIB = os.path.join(HERE, "libldg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
-SOURCES = ["ldg_capi.cu", "ldg_noalloc.cu", "ldg_ops.cpp"]
+SOURCES = ["ldg_capi.cu", "ldg_noalloc.cu", "ldg_ensemble.cu", "ldg_ops.cpp"]
 
 LDG_OK = 0
 LDG_HOST = 0
@@ -95,7 +95,8 @@ class LdgConfig(ctypes.Structure):
         ("Ma", ctypes.c_double), ("cfl", ctypes.c_double), ("precision", ctypes.c_int),
         ("device", ctypes.c_int), ("check_finite", ctypes.c_int), ("use_box", ctypes.c_int),
         ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3),
-        ("reserved", ctypes.c_int * 8),
+        ("perturb_amp", ctypes.c_double), ("seed", ctypes.c_ulonglong), ("instance", ctypes.c_int),
+        ("reserved", ctypes.c_int * 7),
     ]
 
 
@@ -132,6 +133,14 @@ SIGNATURES = {
     "ldg_kernel_times": (_i, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _i, _i]),
     "ldg_probe_fp64_peak": (_i, [_i, _dp]),
     "ldg_rhs_noalloc": (_i, [ctypes.POINTER(LdgConfig), _vp, _vp, _vp]),
+    "ldg_ensemble_create": (_i, [ctypes.POINTER(LdgConfig), _i, ctypes.POINTER(_vp)]),
+    "ldg_ensemble_destroy": (_i, [_vp]),
+    "ldg_ensemble_step": (_i, [_vp, _i]),
+    "ldg_ensemble_get_state": (_i, [_vp, _i, _vp, _i]),
+    "ldg_ensemble_ke_history": (_i, [_vp, _i, _dp, _i, _ip]),
+    "ldg_ensemble_member_info": (_i, [_vp, _i, ctypes.POINTER(LdgInfo)]),
+    "ldg_ensemble_tuning": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_float), _i]),
+    "ldg_ensemble_stream": (_vp, [_vp]),
     "ldg_error_string": (ctypes.c_char_p, [_i]),
     "ldg_last_error_message": (ctypes.c_char_p, []),
     "ldg_abi_version": (_i, []),
@@ -202,7 +211,8 @@ class Solver:
     def __init__(self, p: int, nx: int, ny: int | None = None, nz: int | None = None, *, L: float = 1.0,
                  tf: float | None = None, steps: int | None = None, Re: float = 1600.0, Pr: float = 0.71,
                  gamma: float = 1.4, Ma: float = 0.1, cfl: float = 0.01, device: int = 0,
-                 check_finite: bool = True, dt_snaps: int = 0, box=None, precision: str = "fp64"):
+                 check_finite: bool = True, dt_snaps: int = 0, box=None, precision: str = "fp64",
+                 perturb_amp: float = 0.0, seed: int = 0, instance: int = 0):
         L_ = load()
         cfg = LdgConfig()
         _check(L_.ldg_config_default(ctypes.byref(cfg)), "ldg_config_default")
@@ -216,6 +226,7 @@ class Solver:
         cfg.Re, cfg.Pr, cfg.gamma, cfg.Ma, cfg.cfl = Re, Pr, gamma, Ma, cfl
         cfg.device = device
         cfg.precision = PRECISIONS[precision]
+        cfg.perturb_amp, cfg.seed, cfg.instance = perturb_amp, seed, instance
         cfg.check_finite = 1 if check_finite else 0
         cfg.dt_snaps = dt_snaps
         if box is not None:
@@ -329,3 +340,98 @@ class Solver:
     @property
     def stream(self) -> int:
         return load().ldg_stream(self._h)
+
+
+def make_config(p: int, nx: int, *, steps: int | None = None, tf: float | None = None, L: float = 1.0,
+                Re: float = 1600.0, Pr: float = 0.71, gamma: float = 1.4, Ma: float = 0.1, cfl: float = 0.01,
+                device: int = 0, precision: str = "fp64", perturb_amp: float = 0.0, seed: int = 0,
+                instance: int = 0, check_finite: bool = True) -> LdgConfig:
+    """An ldg_config for an nx^3 periodic Taylor-Green problem."""
+    cfg = LdgConfig()
+    _check(load().ldg_config_default(ctypes.byref(cfg)), "ldg_config_default")
+    cfg.p, cfg.nx, cfg.ny, cfg.nz = p, nx, nx, nx
+    cfg.L = L
+    cfg.tf = tf if tf is not None else tf_for_steps(nx, p, L, steps if steps else 1, cfl)
+    cfg.Re, cfg.Pr, cfg.gamma, cfg.Ma, cfg.cfl = Re, Pr, gamma, Ma, cfl
+    cfg.device, cfg.precision = device, PRECISIONS[precision]
+    cfg.perturb_amp, cfg.seed, cfg.instance = perturb_amp, seed, instance
+    cfg.check_finite = 1 if check_finite else 0
+    return cfg
+
+
+def ensemble_configs(count: int = 64, seed: int = 2024, device: int = 0, steps: int = 1000):
+    """The batched-ensemble inputs: element counts uniform in {8^3, 12^3,
+    16^3, 24^3}, p uniform in {2, 3, 4}, Re log-uniform in [400, 3200],
+    Ma = 0.1, velocity perturbation of amplitude 1e-2 V0 over wavenumbers
+    1-4 with phases keyed by (seed, member)."""
+    rng = np.random.default_rng(seed)
+    cfgs = []
+    for i in range(count):
+        nx = int(rng.choice([8, 12, 16, 24]))
+        p = int(rng.choice([2, 3, 4]))
+        Re = float(np.exp(rng.uniform(np.log(400.0), np.log(3200.0))))
+        cfgs.append(make_config(p, nx, steps=steps, Re=Re, Ma=0.1, device=device, perturb_amp=1e-2,
+                                seed=seed, instance=i))
+    return cfgs
+
+
+class Ensemble:
+    """Members advanced together by ldg_ensemble_* (one persistent launch per
+    RK4 stage, CUDA-graph steps)."""
+
+    def __init__(self, cfgs):
+        L_ = load()
+        arr = (LdgConfig * len(cfgs))(*cfgs)
+        h = ctypes.c_void_p()
+        _check(L_.ldg_ensemble_create(arr, len(cfgs), ctypes.byref(h)), "ldg_ensemble_create")
+        self._h = h
+        self.cfgs = list(cfgs)
+        self.count = len(cfgs)
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ldg_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def info(self, member: int) -> LdgInfo:
+        info = LdgInfo()
+        _check(load().ldg_ensemble_member_info(self._h, member, ctypes.byref(info)), "ldg_ensemble_member_info")
+        return info
+
+    def step(self, nsteps: int = 1) -> None:
+        _check(load().ldg_ensemble_step(self._h, nsteps), "ldg_ensemble_step")
+
+    def get_state(self, member: int) -> np.ndarray:
+        info = self.info(member)
+        out = np.empty((info.nelements, 5, info.dofs))
+        _check(load().ldg_ensemble_get_state(self._h, member, out.ctypes.data, LDG_HOST), "ldg_ensemble_get_state")
+        return out
+
+    def ke_history(self, member: int) -> np.ndarray:
+        cnt = ctypes.c_int()
+        _check(load().ldg_ensemble_ke_history(self._h, member, None, 0, ctypes.byref(cnt)), "ke_history")
+        out = np.zeros(cnt.value)
+        if cnt.value:
+            _check(load().ldg_ensemble_ke_history(self._h, member, out.ctypes.data_as(_dp), cnt.value,
+                                                  ctypes.byref(cnt)), "ke_history")
+        return out
+
+    def tuning(self):
+        t, g = ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_float * 8)()
+        _check(load().ldg_ensemble_tuning(self._h, ctypes.byref(t), ctypes.byref(g), ms, 8), "ldg_ensemble_tuning")
+        return {"threads_per_cta": t.value, "persistent_ctas": g.value,
+                "stage_ms": {f"{128 * (1 + k // 4)}x{k % 4}": ms[k] for k in range(8)}}
+
+    @property
+    def stream(self) -> int:
+        return load().ldg_ensemble_stream(self._h)

@@ -549,8 +549,15 @@ int ldgo_get_operator(const ldgo* o, int which, double* out) {
 }
 
 /* Taylor-Green initial condition at the element nodes (solver.cpp:194-236,
- * node coordinates mesh.cpp:127-151,389-408). */
-void ldgo_initial_condition(const ldgo* o, double* u) {
+ * node coordinates mesh.cpp:127-151,389-408), plus an optional velocity
+ * perturbation amp * sum_{k=1..4} sum_d sin(k x_d / L + phi[c][k-1][d])
+ * (ensemble inputs; phi as 36 doubles, amp = 0 for none). */
+static void initial_condition_impl(const ldgo* o, double* u, double amp, const double* phi);
+void ldgo_initial_condition(const ldgo* o, double* u) { initial_condition_impl(o, u, 0.0, NULL); }
+void ldgo_initial_condition_perturbed(const ldgo* o, double* u, double amp, const double* phi) {
+  initial_condition_impl(o, u, amp, phi);
+}
+static void initial_condition_impl(const ldgo* o, double* u, double amp, const double* phi) {
   int N = o->N, n = o->n, p = o->p;
   double cheb[16];
   chebyshev(p, cheb);
@@ -578,6 +585,13 @@ void ldgo_initial_condition(const ldgo* o, double* u) {
               uk[v + 1 * n] = o->rho0 * o->V0 * sin(x / L) * cos(y / L) * cos(z / L);
               uk[v + 2 * n] = -o->rho0 * o->V0 * cos(x / L) * sin(y / L) * cos(z / L);
               uk[v + 3 * n] = 0 * o->rho0;
+              if (amp != 0.0) {
+                double X[3] = {x / L, y / L, z / L}, dv[3] = {0, 0, 0};
+                for (int cpt = 0; cpt < 3; ++cpt)
+                  for (int k = 1; k <= 4; ++k)
+                    for (int d = 0; d < 3; ++d) dv[cpt] += sin(k * X[d] + phi[cpt * 12 + (k - 1) * 3 + d]);
+                for (int cpt = 0; cpt < 3; ++cpt) uk[v + (1 + cpt) * n] += o->rho0 * amp * dv[cpt];
+              }
               uk[v + 4 * n] = pr / (o->gamma - 1) + (uk[v + 1 * n] * uk[v + 1 * n] + uk[v + 2 * n] * uk[v + 2 * n] +
                                                      uk[v + 3 * n] * uk[v + 3 * n]) / (2.0 * uk[v + 0 * n]);
             }

@@ -58,6 +58,7 @@ def lib():
         L.ldgo_nelements.restype = i
         L.ldgo_nelements.argtypes = [vp]
         L.ldgo_initial_condition.argtypes = [vp, dp]
+        L.ldgo_initial_condition_perturbed.argtypes = [vp, dp, d, dp]
         L.ldgo_rhs.argtypes = [vp, dp, dp]
         L.ldgo_step.argtypes = [vp, dp, i, dp]
         L.ldgo_compute_ke.restype = d
@@ -78,6 +79,30 @@ def tf_for_steps(nx: int, p: int, L: float, steps: int) -> float:
     while math.ceil(tf / dt0) > steps:
         tf = np.nextafter(tf, 0.0)
     return float(tf)
+
+
+_MASK = (1 << 64) - 1
+
+
+def splitmix64(z: int) -> int:
+    """SplitMix64 (Steele, Lea & Flood 2014)."""
+    z = (z + 0x9E3779B97F4A7C15) & _MASK
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK
+    return z ^ (z >> 31)
+
+
+def perturbation_phases(seed: int, instance: int) -> np.ndarray:
+    """Phases [component][wavenumber-1][direction] of the seeded velocity
+    perturbation of the ensemble inputs."""
+    base = splitmix64(seed ^ splitmix64((0x4C44470000000000 + instance) & _MASK))
+    phi = np.zeros((3, 4, 3))
+    for c in range(3):
+        for k in range(4):
+            for d in range(3):
+                r = splitmix64((base + c * 16 + k * 4 + d) & _MASK)
+                phi[c, k, d] = 2.0 * math.pi * (r >> 11) * (1.0 / 9007199254740992.0)
+    return phi
 
 
 def find_openblas() -> str | None:
@@ -131,9 +156,13 @@ class Oracle:
         lib().ldgo_set_dt(self._h, dt)
         self.dt = dt
 
-    def initial_condition(self) -> np.ndarray:
+    def initial_condition(self, perturb_amp: float = 0.0, seed: int = 0, instance: int = 0) -> np.ndarray:
         u = np.zeros(self.shape)
-        lib().ldgo_initial_condition(self._h, _ptr(u))
+        if perturb_amp:
+            phi = np.ascontiguousarray(perturbation_phases(seed, instance).ravel())
+            lib().ldgo_initial_condition_perturbed(self._h, _ptr(u), perturb_amp / 12.0, _ptr(phi))
+        else:
+            lib().ldgo_initial_condition(self._h, _ptr(u))
         return u
 
     def rhs(self, u: np.ndarray) -> np.ndarray:
