@@ -201,6 +201,51 @@ int ldg_ensemble_tuning(const ldg_ensemble* e, int* threads_per_cta, int* persis
                         int max);
 void* ldg_ensemble_stream(ldg_ensemble* e);
 
+/* ---- Learned closure.  No reference counterpart.  A per-element MLP
+ * (features: the coarse element's 5 conserved variables and 15 gradient
+ * components at its (p+1)^3 Gauss points; two hidden GELU layers; output:
+ * a 5 x (p+1)^3 RHS correction) trained on the GPU by the library's own
+ * BF16 tensor-core kernels (FP32 accumulation, FP32 master weights, Adam)
+ * to map a coarse solver's RHS onto the L2 projection of a fine FP64
+ * solver's RHS.  Attached to a coarse FP64 solver, every RK stage adds the
+ * correction before the update; detached (or for an element whose
+ * prediction is not finite) the plain LDG operator is used. */
+typedef struct ldg_closure ldg_closure;
+int ldg_closure_create(int p_coarse, int hidden, unsigned long long seed, int device, ldg_closure** out);
+int ldg_closure_destroy(ldg_closure* c);
+/* One training sample per coarse element from the fine solver's current
+ * state: the fine state and RHS L2-projected onto the coarse mesh (the fine
+ * mesh must refine the coarse one uniformly, same domain), the coarse
+ * gradient and RHS of the projected state.  Both solvers FP64. */
+int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse);
+int ldg_closure_sample_count(const ldg_closure* c, long long* count);
+/* Per-channel normalisation statistics from samples [first, first+count). */
+int ldg_closure_finalize_data(ldg_closure* c, long long first, long long count);
+/* iters Adam steps on random batches from samples [first, first+count);
+ * losses[i] (optional) receives the normalised MSE of step i. */
+int ldg_closure_train(ldg_closure* c, long long first, long long count, int iters, int batch, float lr,
+                      unsigned long long seed, float* losses);
+/* Mean squared RHS error (in units of the target's channel deviation) on
+ * samples [first, first+count): of the plain coarse operator and with the
+ * closure. */
+int ldg_closure_evaluate(ldg_closure* c, long long first, long long count, double* err_plain, double* err_closure);
+int ldg_closure_param_count(const ldg_closure* c, long long* count);
+int ldg_closure_get_params(ldg_closure* c, float* out);
+int ldg_closure_set_params(ldg_closure* c, const float* in);
+/* mean[20], std[20] of the input channels, mean[5], std[5] of the outputs */
+int ldg_closure_get_stats(ldg_closure* c, float* out50);
+/* Raw network on normalised host batches: y = MLP(x), and the parameter
+ * gradient of sum(y * dy) (layout of ldg_closure_get_params). */
+int ldg_closure_mlp_forward(ldg_closure* c, const float* x, float* y, int batch);
+int ldg_closure_mlp_backward(ldg_closure* c, const float* x, const float* dy, int batch, float* grad);
+/* Raw samples [first, first+count): features (count x 20 (p+1)^3) and
+ * targets (count x 5 (p+1)^3) as float; either pointer may be NULL. */
+int ldg_closure_get_samples(ldg_closure* c, long long first, long long count, float* X, float* Y);
+/* Elements whose correction was dropped (non-finite prediction). */
+int ldg_closure_fallbacks(ldg_closure* c, long long* count);
+/* Attach (c) or detach (NULL) a closure on a coarse FP64 solver. */
+int ldg_solver_attach_closure(ldg_solver* s, ldg_closure* c);
+
 /* RHS evaluation without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot let the library allocate
  * device memory -- an application whose memory is owned by its own arena or

@@ -14,6 +14,7 @@
 #include "ldg_kernels.cuh"
 #include "ldg_ops.hpp"
 #include "ldg_problem.hpp"
+#include "ldg_closure.hpp"
 
 using namespace ldg;
 
@@ -54,6 +55,8 @@ struct ldg_solver {
   OpsT<double> o64;  // arithmetic constants of the FP64 path
   OpsT<dd> odd;      // ... of the FP32-pair (mixed) path
   bool mixed = false;
+  ldg_closure* closure = nullptr;  // learned RHS correction (FP64 path), or none
+  double* Kadd = nullptr;          // its per-stage output
   Ops1D o1;
   double xi[kMaxN];  // CGL nodes as the reference computes them
   double lo[3], hi[3];
@@ -239,6 +242,7 @@ struct StageCall {
   void* Unext = nullptr;
   void* Tu_out = nullptr;
   double* Kout = nullptr;
+  const double* Kadd = nullptr;
   double* diag = nullptr;
   int* flag = nullptr;
   double cacc = 0, cnext = 0;
@@ -278,6 +282,7 @@ cudaError_t launch_rhs(const StageCall& c, const DevOps& ops, const OpsT<T>& o, 
   a.Unext = (S*)c.Unext;
   a.Tu_out = (S*)c.Tu_out;
   a.Kout = c.Kout;
+  a.Kadd = c.Kadd;
   a.diag = c.diag;
   a.flag = c.flag;
   a.cacc = c.cacc;
@@ -318,6 +323,7 @@ void free_all(ldg_solver* s) {
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (s->flag) cudaFree(s->flag);
+  if (s->Kadd) cudaFree(s->Kadd);
   for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
   s->ev.clear();
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -567,6 +573,79 @@ cudaError_t launch_traces_fp64(int N, const double* U, double* Tu, int nE, const
 
 }  // namespace ldg
 
+namespace ldg {
+
+SolverView solver_view(ldg_solver* s) {
+  SolverView v;
+  v.N = s->N;
+  v.n = s->n;
+  v.nf = s->nf;
+  v.nE = s->nE;
+  v.nx = s->cfg.nx;
+  v.ny = s->cfg.ny;
+  v.nz = s->cfg.nz;
+  v.p = s->cfg.p;
+  v.ops = &s->ops;
+  v.o64 = &s->o64;
+  v.stream = s->stream;
+  v.device = s->cfg.device;
+  v.mixed = s->mixed;
+  v.Un = s->Un;
+  v.Q = s->Q;
+  return v;
+}
+
+// K = rhs(U) in the Gauss basis (FP64), U any Gauss-space state of this
+// solver's mesh; the solver's state is not touched.  The gradient of U is
+// left in s->Q (valid until the next call on s).  Uses the spare trace
+// buffer, Tq and Us as scratch.
+int solver_rhs_gauss(ldg_solver* s, const double* U, double* K) {
+  if (s->mixed) return fail(LDG_ERR_UNSUPPORTED, "closure data needs FP64 solvers");
+  double* Tu = s->Tu[1 - s->cur];
+  LDG_CUDA(s_traces(s, false, U, nullptr, Tu));
+  LDG_CUDA(s_grad(s, false, U, Tu, nullptr));
+  StageCall c;
+  c.Us = U;
+  c.Q = s->Q;
+  c.Tu = Tu;
+  c.Tq = s->Tq;
+  c.Kout = K;
+  c.stage = -1;
+  LDG_CUDA(s_rhs(s, false, c));
+  return LDG_OK;
+}
+
+// Makes U (Gauss basis) the solver's state.
+int solver_set_gauss_state(ldg_solver* s, const double* U) {
+  LDG_CUDA(cudaMemcpyAsync(s->Un, U, state_count(s) * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+  LDG_CUDA(s_traces(s, s->mixed, s->Un, s->mixed ? (void*)s->Us : nullptr, s->Tu[s->cur]));
+  return LDG_OK;
+}
+
+}  // namespace ldg
+
+extern "C" {
+
+int ldg_solver_attach_closure(ldg_solver* s, ldg_closure* c) {
+  if (!s) return fail(LDG_ERR_INVALID, "null solver");
+  if (!c) {  // detach: the plain LDG operator
+    s->closure = nullptr;
+    return LDG_OK;
+  }
+  if (s->mixed) return fail(LDG_ERR_UNSUPPORTED, "the closure corrects FP64 solvers");
+  int st = closure_check_solver(c, solver_view(s));
+  if (st) return st;
+  if (!s->Kadd) {
+    double* p = nullptr;
+    if ((st = dmalloc(s, &p, state_count(s)))) return st;
+    s->Kadd = p;
+  }
+  s->closure = c;
+  return LDG_OK;
+}
+
+}  // extern "C"
+
 extern "C" {
 
 int ldg_abi_version(void) { return LDG_ABI_VERSION; }
@@ -794,7 +873,12 @@ int ldg_step(ldg_solver* s, int nsteps) {
       LDG_CUDA(tic(s, 0));
       LDG_CUDA(s_grad(s, mixed, Uin, Tu_in, nullptr));
       LDG_CUDA(toc(s));
+      if (s->closure) {
+        int cst = closure_correction(s->closure, solver_view(s), (const double*)Uin, s->Q, s->Kadd, s->stream);
+        if (cst) return cst;
+      }
       StageCall c;
+      c.Kadd = s->closure ? s->Kadd : nullptr;
       c.Us = Uin;
       c.Q = s->Q;
       c.Tu = Tu_in;

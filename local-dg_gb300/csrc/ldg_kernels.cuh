@@ -356,6 +356,7 @@ struct StageArgs {
                       // the mixed path's pair copy of the new state
   S* Tu_out;          // traces of Unext (or of Uacc on the last stage)
   double* Kout;       // raw RHS output (rhs-only mode)
+  const double* Kadd; // optional additive RHS term (learned closure), same layout as U
   double* diag;       // per-element [ke_ref, ke] on the last stage (FP64 path)
   int* flag;          // nonzero if a non-finite value was produced
   double cacc;        // dt * b_s
@@ -473,13 +474,16 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
     const long e = e0 + es;
     if (a.stage < 0) {
 #pragma unroll
-      for (int v = 0; v < kNS; ++v) a.Kout[(e * kNS + v) * n + q] = R::to_f64(K[v]);
+      for (int v = 0; v < kNS; ++v) {
+        const long idx = (e * kNS + v) * n + q;
+        a.Kout[idx] = a.Kadd ? R::to_f64(K[v]) + a.Kadd[idx] : R::to_f64(K[v]);
+      }
     } else {
       bool bad = false;
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
         const long idx = (e * kNS + v) * n + q;
-        const double kd = R::to_f64(K[v]);
+        const double kd = a.Kadd ? R::to_f64(K[v]) + a.Kadd[idx] : R::to_f64(K[v]);
         const double un = a.Un[idx];
         const double acc0 = a.stage == 0 ? un : a.Uacc[idx];
         const double uacc = acc0 + a.cacc * kd;

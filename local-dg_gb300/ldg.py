@@ -31,7 +31,7 @@ LIB = os.path.join(HERE, "libldg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
-SOURCES = ["ldg_capi.cu", "ldg_noalloc.cu", "ldg_ensemble.cu", "ldg_ops.cpp"]
+SOURCES = ["ldg_capi.cu", "ldg_noalloc.cu", "ldg_ensemble.cu", "ldg_closure.cu", "ldg_ops.cpp"]
 
 LDG_OK = 0
 LDG_HOST = 0
@@ -141,6 +141,25 @@ SIGNATURES = {
     "ldg_ensemble_member_info": (_i, [_vp, _i, ctypes.POINTER(LdgInfo)]),
     "ldg_ensemble_tuning": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_float), _i]),
     "ldg_ensemble_stream": (_vp, [_vp]),
+    "ldg_closure_create": (_i, [_i, _i, ctypes.c_ulonglong, _i, ctypes.POINTER(_vp)]),
+    "ldg_closure_destroy": (_i, [_vp]),
+    "ldg_closure_add_samples": (_i, [_vp, _vp, _vp]),
+    "ldg_closure_sample_count": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "ldg_closure_finalize_data": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong]),
+    "ldg_closure_train": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, _i, _i, ctypes.c_float,
+                               ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_float)]),
+    "ldg_closure_evaluate": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, _dp, _dp]),
+    "ldg_closure_param_count": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "ldg_closure_get_params": (_i, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "ldg_closure_set_params": (_i, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "ldg_closure_get_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "ldg_closure_mlp_forward": (_i, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _i]),
+    "ldg_closure_mlp_backward": (_i, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _i,
+                                      ctypes.POINTER(ctypes.c_float)]),
+    "ldg_closure_fallbacks": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "ldg_closure_get_samples": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(ctypes.c_float),
+                                     ctypes.POINTER(ctypes.c_float)]),
+    "ldg_solver_attach_closure": (_i, [_vp, _vp]),
     "ldg_error_string": (ctypes.c_char_p, [_i]),
     "ldg_last_error_message": (ctypes.c_char_p, []),
     "ldg_abi_version": (_i, []),
@@ -327,6 +346,12 @@ class Solver:
     def synchronize(self) -> None:
         _check(load().ldg_synchronize(self._h), "ldg_synchronize")
 
+    def attach_closure(self, closure) -> None:
+        """Adds the closure's correction to every RK stage (None: plain LDG)."""
+        _check(load().ldg_solver_attach_closure(self._h, closure._h if closure is not None else None),
+               "ldg_solver_attach_closure")
+        self._closure = closure
+
     def enable_kernel_timing(self, enable: bool = True) -> None:
         _check(load().ldg_enable_kernel_timing(self._h, 1 if enable else 0), "ldg_enable_kernel_timing")
 
@@ -373,6 +398,106 @@ def ensemble_configs(count: int = 64, seed: int = 2024, device: int = 0, steps: 
         cfgs.append(make_config(p, nx, steps=steps, Re=Re, Ma=0.1, device=device, perturb_amp=1e-2,
                                 seed=seed, instance=i))
     return cfgs
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class Closure:
+    """The learned RHS closure (ldg_closure_*)."""
+
+    def __init__(self, p: int = 2, hidden: int = 128, seed: int = 0, device: int = 0):
+        h = ctypes.c_void_p()
+        _check(load().ldg_closure_create(p, hidden, seed, device, ctypes.byref(h)), "ldg_closure_create")
+        self._h = h
+        self.p, self.hidden = p, hidden
+        n = (p + 1) ** 3
+        self.in_dim, self.out_dim = 20 * n, 5 * n
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ldg_closure_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_samples(self, fine: "Solver", coarse: "Solver") -> None:
+        _check(load().ldg_closure_add_samples(self._h, fine._h, coarse._h), "ldg_closure_add_samples")
+
+    @property
+    def samples(self) -> int:
+        c = ctypes.c_longlong()
+        _check(load().ldg_closure_sample_count(self._h, ctypes.byref(c)), "ldg_closure_sample_count")
+        return c.value
+
+    def finalize(self, first: int, count: int) -> None:
+        _check(load().ldg_closure_finalize_data(self._h, first, count), "ldg_closure_finalize_data")
+
+    def train(self, first: int, count: int, iters: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0):
+        losses = np.zeros(max(iters, 1), dtype=np.float32)
+        _check(load().ldg_closure_train(self._h, first, count, iters, batch, lr, seed, _fp(losses)),
+               "ldg_closure_train")
+        return losses[:iters]
+
+    def evaluate(self, first: int, count: int):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(load().ldg_closure_evaluate(self._h, first, count, ctypes.byref(a), ctypes.byref(b)),
+               "ldg_closure_evaluate")
+        return a.value, b.value
+
+    @property
+    def n_params(self) -> int:
+        c = ctypes.c_longlong()
+        _check(load().ldg_closure_param_count(self._h, ctypes.byref(c)), "ldg_closure_param_count")
+        return c.value
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        _check(load().ldg_closure_get_params(self._h, _fp(out)), "ldg_closure_get_params")
+        return out
+
+    def set_params(self, theta) -> None:
+        theta = np.ascontiguousarray(theta, dtype=np.float32)
+        _check(load().ldg_closure_set_params(self._h, _fp(theta)), "ldg_closure_set_params")
+
+    def stats(self) -> np.ndarray:
+        out = np.zeros(50, dtype=np.float32)
+        _check(load().ldg_closure_get_stats(self._h, _fp(out)), "ldg_closure_get_stats")
+        return out
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros((x.shape[0], self.out_dim), dtype=np.float32)
+        _check(load().ldg_closure_mlp_forward(self._h, _fp(x), _fp(y), x.shape[0]), "ldg_closure_mlp_forward")
+        return y
+
+    def backward(self, x, dy) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        dy = np.ascontiguousarray(dy, dtype=np.float32)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        _check(load().ldg_closure_mlp_backward(self._h, _fp(x), _fp(dy), x.shape[0], _fp(g)),
+               "ldg_closure_mlp_backward")
+        return g
+
+    def get_samples(self, first: int, count: int):
+        X = np.zeros((count, self.in_dim), dtype=np.float32)
+        Y = np.zeros((count, self.out_dim), dtype=np.float32)
+        _check(load().ldg_closure_get_samples(self._h, first, count, _fp(X), _fp(Y)), "ldg_closure_get_samples")
+        return X, Y
+
+    @property
+    def fallbacks(self) -> int:
+        c = ctypes.c_longlong()
+        _check(load().ldg_closure_fallbacks(self._h, ctypes.byref(c)), "ldg_closure_fallbacks")
+        return c.value
 
 
 class Ensemble:
