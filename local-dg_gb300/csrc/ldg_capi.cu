@@ -272,7 +272,7 @@ cudaError_t launch_grad(const void* U, const void* Tu, void* Q, void* Tq, double
 template <int N, class T>
 cudaError_t launch_rhs(const StageCall& c, const DevOps& ops, const OpsT<T>& o, cudaStream_t st) {
   using S = typename Real<T>::S;
-  StageArgs<T> a;
+  StageArgs<T> a{};
   a.Us = (const S*)c.Us;
   a.Q = (const S*)c.Q;
   a.Tu = (const S*)c.Tu;

@@ -89,7 +89,7 @@ __device__ void run_item(const Member& m, const Item& it, int stage, int cur, in
   if (it.phase == 0) {
     grad_body<N, double, E>(Uin, Tu_in, m.Q, m.Tq, nullptr, m.ops, m.o, it.e0, it.ne, smem);
   } else {
-    StageArgs<double> a;
+    StageArgs<double> a{};
     a.Us = Uin;
     a.Q = m.Q;
     a.Tu = Tu_in;

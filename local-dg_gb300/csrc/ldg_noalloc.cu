@@ -88,7 +88,7 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   k_transform<N><<<grid, C::T, sm_tr, st>>>(u, U, nE, kNS, ops, 0);
   k_traces<N, double><<<grid, C::T, sm_trc, st>>>(U, nullptr, Tu, nE, o);
   k_grad<N, double><<<grid, C::T, sm_g, st>>>(U, Tu, Q, Tq, nullptr, ops, o);
-  StageArgs<double> a;
+  StageArgs<double> a{};
   std::memset(&a, 0, sizeof(a));
   a.Us = U;
   a.Q = Q;
