@@ -261,8 +261,8 @@ int ldg_solver_attach_closure(ldg_solver* s, ldg_closure* c);
  * Intermediate buffers live in one fixed file-scope device array of
  * LDG_NOALLOC_SCRATCH_BYTES (64 MiB), which every GPU that loads the
  * library holds until the process exits.  A mesh whose buffers need more
- * (nElements * (20 (p+1)^3 + 75 (p+1)^2) * 8 bytes, i.e. about 1900
- * elements at p=4, 3400 at p=3, 6900 at p=2) is rejected with LDG_ERR_INVALID.
+ * (nElements * (20 (p+1)^3 + 90 (p+1)^2) * 8 bytes, i.e. about 1760
+ * elements at p=4, 3080 at p=3, 6210 at p=2) is rejected with LDG_ERR_INVALID.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress, with that device current); make that first call
  * before any stream capture.  All calls share the array and it keeps the

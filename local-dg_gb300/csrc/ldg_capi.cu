@@ -63,7 +63,7 @@ struct ldg_solver {
   double p0 = 0, T0 = 0, R = 8.314, rho0 = 1.0, V0 = 1.0;
   cudaStream_t stream = nullptr;
   // device buffers
-  double *Un = nullptr, *Uacc = nullptr, *Us = nullptr, *Q = nullptr, *Tq = nullptr;
+  double *Un = nullptr, *Uacc = nullptr, *Us = nullptr, *Q = nullptr, *Tq = nullptr, *Fm = nullptr;
   double* Tu[2] = {nullptr, nullptr};
   double *nodal = nullptr, *diag = nullptr, *ens = nullptr, *ke_dev = nullptr, *red = nullptr;
   int* flag = nullptr;
@@ -187,7 +187,7 @@ template <int N>
 size_t smem_traces() { return sizeof(double) * Cfg<N>::EPC * kNS * Cfg<N>::n; }
 template <int N>
 size_t smem_grad() {
-  return sizeof(double) * Cfg<N>::EPC * (kNS * Cfg<N>::n + kNQ * Cfg<N>::n + 6 * kNS * Cfg<N>::nf + Cfg<N>::n);
+  return sizeof(double) * Cfg<N>::EPC * (kNS * Cfg<N>::n + kNQ * Cfg<N>::n + 9 * kNS * Cfg<N>::nf + Cfg<N>::n);
 }
 template <int N>
 size_t smem_rhs() {
@@ -237,6 +237,7 @@ struct StageCall {
   const void* Q = nullptr;
   const void* Tu = nullptr;
   const void* Tq = nullptr;
+  const void* Fm = nullptr;
   const double* Un = nullptr;
   double* Uacc = nullptr;
   void* Unext = nullptr;
@@ -262,11 +263,11 @@ cudaError_t launch_traces(const double* U, void* Ucopy, void* Tu, int nE, const 
   return cudaGetLastError();
 }
 template <int N, class T>
-cudaError_t launch_grad(const void* U, const void* Tu, void* Q, void* Tq, double* ens, const DevOps& ops,
-                        const OpsT<T>& o, cudaStream_t st) {
+cudaError_t launch_grad(const void* U, const void* Tu, void* Q, void* Tq, void* Fm, double* ens,
+                        const DevOps& ops, const OpsT<T>& o, cudaStream_t st) {
   using S = typename Real<T>::S;
   k_grad<N, T><<<grid_for<N>(ops.nE), Cfg<N>::T, smem_grad<N>(), st>>>((const S*)U, (const S*)Tu, (S*)Q,
-                                                                        (S*)Tq, ens, ops, o);
+                                                                        (S*)Tq, (S*)Fm, ens, ops, o);
   return cudaGetLastError();
 }
 template <int N, class T>
@@ -277,6 +278,7 @@ cudaError_t launch_rhs(const StageCall& c, const DevOps& ops, const OpsT<T>& o, 
   a.Q = (const S*)c.Q;
   a.Tu = (const S*)c.Tu;
   a.Tq = (const S*)c.Tq;
+  a.Fm = (const S*)c.Fm;
   a.Un = c.Un;
   a.Uacc = c.Uacc;
   a.Unext = (S*)c.Unext;
@@ -319,7 +321,7 @@ cudaError_t d_ke(int N, const double* U, double* diag, const DevOps& ops, cudaSt
 
 // ---------------------------------------------------------------- helpers
 void free_all(ldg_solver* s) {
-  double* bufs[] = {s->Un, s->Uacc, s->Us, s->Q, s->Tq, s->Tu[0], s->Tu[1], s->nodal, s->diag, s->ens, s->ke_dev, s->red};
+  double* bufs[] = {s->Un, s->Uacc, s->Us, s->Q, s->Tq, s->Fm, s->Tu[0], s->Tu[1], s->nodal, s->diag, s->ens, s->ke_dev, s->red};
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (s->flag) cudaFree(s->flag);
@@ -412,8 +414,8 @@ cudaError_t s_traces(ldg_solver* s, bool mixed, const double* U, void* Ucopy, vo
   LDG_DISPATCH(s->N, (launch_traces<NN, double>(U, Ucopy, Tu, s->nE, s->o64, s->stream)));
 }
 cudaError_t s_grad(ldg_solver* s, bool mixed, const void* U, const void* Tu, double* ens) {
-  if (mixed) LDG_DISPATCH(s->N, (launch_grad<NN, dd>(U, Tu, s->Q, s->Tq, ens, s->ops, s->odd, s->stream)));
-  LDG_DISPATCH(s->N, (launch_grad<NN, double>(U, Tu, s->Q, s->Tq, ens, s->ops, s->o64, s->stream)));
+  if (mixed) LDG_DISPATCH(s->N, (launch_grad<NN, dd>(U, Tu, s->Q, s->Tq, s->Fm, ens, s->ops, s->odd, s->stream)));
+  LDG_DISPATCH(s->N, (launch_grad<NN, double>(U, Tu, s->Q, s->Tq, s->Fm, ens, s->ops, s->o64, s->stream)));
 }
 cudaError_t s_rhs(ldg_solver* s, bool mixed, const StageCall& c) {
   if (mixed) LDG_DISPATCH(s->N, (launch_rhs<NN, dd>(c, s->ops, s->odd, s->stream)));
@@ -609,6 +611,7 @@ int solver_rhs_gauss(ldg_solver* s, const double* U, double* K) {
   c.Q = s->Q;
   c.Tu = Tu;
   c.Tq = s->Tq;
+  c.Fm = s->Fm;
   c.Kout = K;
   c.stage = -1;
   LDG_CUDA(s_rhs(s, false, c));
@@ -731,6 +734,7 @@ int ldg_create(const ldg_config* cfg, ldg_solver** out) {
   const size_t nE = s->nE;
   if ((st = dmalloc(s, &s->Un, ns)) || (st = dmalloc(s, &s->Uacc, ns)) || (st = dmalloc(s, &s->Us, ns)) ||
       (st = dmalloc(s, &s->Q, nE * kNQ * s->n)) || (st = dmalloc(s, &s->Tq, nE * 3 * kNQ * s->nf)) ||
+      (st = dmalloc(s, &s->Fm, nE * 3 * kNS * s->nf)) ||
       (st = dmalloc(s, &s->Tu[0], nE * 6 * kNS * s->nf)) || (st = dmalloc(s, &s->Tu[1], nE * 6 * kNS * s->nf)) ||
       (st = dmalloc(s, &s->nodal, ns)) || (st = dmalloc(s, &s->diag, nE * 2)) || (st = dmalloc(s, &s->ens, nE)) ||
       (st = dmalloc(s, &s->red, 8))) {
@@ -844,6 +848,7 @@ int ldg_rhs(ldg_solver* s, const double* u_curr, double* k, int where) {
   c.Q = s->Q;
   c.Tu = Tu;
   c.Tq = s->Tq;
+  c.Fm = s->Fm;
   c.Kout = s->Us;  // FP64 RHS in the stage buffer (restored below on the mixed path)
   c.stage = -1;
   LDG_CUDA(s_rhs(s, s->mixed, c));
@@ -883,6 +888,8 @@ int ldg_step(ldg_solver* s, int nsteps) {
       c.Q = s->Q;
       c.Tu = Tu_in;
       c.Tq = s->Tq;
+      c.Fm = s->Fm;
+  c.Fm = s->Fm;
       c.Un = s->Un;
       c.Uacc = s->Uacc;
       c.Unext = (stage < 3 || mixed) ? (void*)s->Us : nullptr;

@@ -43,9 +43,13 @@ struct DevOps {
 // The arithmetic constants of the step kernels in the type they compute in.
 template <class T>
 struct OpsT {
-  T A[kDevMaxN * kDevMaxN];
-  T lp[kDevMaxN], lm[kDevMaxN], Lp[kDevMaxN], Lm[kDevMaxN];
-  T ia[3];
+  T lp[kDevMaxN], lm[kDevMaxN];
+  // Per direction l, pre-scaled by 1/alpha_l so the kernels spend no
+  // multiplications on the element size: As = A / alpha_l, Lps = Lp /
+  // alpha_l, Lms = Lm / alpha_l (gradient pass), and their negations for the
+  // RHS lifts.
+  T As[3][kDevMaxN * kDevMaxN];
+  T Lps[3][kDevMaxN], Lms[3][kDevMaxN];
   T g1, hg1, gamma, inv_re, kappa, two3, one;
 };
 
@@ -57,14 +61,17 @@ template <class T>
 inline OpsT<T> make_opst(const DevOps& d, int N) {
   OpsT<T> o;
   const T* tag = nullptr;
-  for (int i = 0; i < kDevMaxN * kDevMaxN; ++i) o.A[i] = host_cast(i < N * N ? d.A[i] : 0.0, tag);
   for (int i = 0; i < kDevMaxN; ++i) {
     o.lp[i] = host_cast(d.lp[i], tag);
     o.lm[i] = host_cast(d.lm[i], tag);
-    o.Lp[i] = host_cast(d.Lp[i], tag);
-    o.Lm[i] = host_cast(d.Lm[i], tag);
   }
-  for (int l = 0; l < 3; ++l) o.ia[l] = host_cast(d.ia[l], tag);
+  for (int l = 0; l < 3; ++l) {
+    for (int i = 0; i < kDevMaxN * kDevMaxN; ++i) o.As[l][i] = host_cast(i < N * N ? d.A[i] * d.ia[l] : 0.0, tag);
+    for (int i = 0; i < kDevMaxN; ++i) {
+      o.Lps[l][i] = host_cast(d.Lp[i] * d.ia[l], tag);
+      o.Lms[l][i] = host_cast(d.Lm[i] * d.ia[l], tag);
+    }
+  }
   o.g1 = host_cast(d.g1, tag);
   o.hg1 = host_cast(0.5 * d.g1, tag);
   o.gamma = host_cast(d.gamma, tag);
@@ -180,6 +187,20 @@ __device__ __forceinline__ void visc_column(const ViscPre<T>& P, const OpsT<T>& 
   F[2] = tau[1] * o.inv_re;
   F[3] = tau[2] * o.inv_re;
   F[4] = (tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + o.kappa * P.de[j]) * o.inv_re;
+}
+
+// F -= column j of the viscous flux, fused (FMA) into the Euler column.
+template <int j, class T>
+__device__ __forceinline__ void sub_visc_column(const ViscPre<T>& P, const OpsT<T>& o, T F[kNS]) {
+  T tau[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) tau[i] = P.G[i][j] + P.G[j][i];
+  tau[j] -= o.two3 * P.div;
+  const T mre = -o.inv_re;
+  F[1] = fma(tau[0], mre, F[1]);
+  F[2] = fma(tau[1], mre, F[2]);
+  F[3] = fma(tau[2], mre, F[3]);
+  F[4] = fma(tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + o.kappa * P.de[j], mre, F[4]);
 }
 
 // Roe flux F*(uN, uK, n) seen from element K with n = s e_l

@@ -61,6 +61,7 @@ struct Member {
   double* Us;
   double* Q;
   double* Tq;
+  double* Fm;
   double* Tu[2];
   double* diag;
   double cacc[4];
@@ -87,13 +88,14 @@ __device__ void run_item(const Member& m, const Item& it, int stage, int cur, in
   double* Tu_out = m.Tu[(stage & 1) ? cur : 1 - cur];
   const double* Uin = stage == 0 ? m.Un : m.Us;
   if (it.phase == 0) {
-    grad_body<N, double, E>(Uin, Tu_in, m.Q, m.Tq, nullptr, m.ops, m.o, it.e0, it.ne, smem);
+    grad_body<N, double, E>(Uin, Tu_in, m.Q, m.Tq, m.Fm, nullptr, m.ops, m.o, it.e0, it.ne, smem);
   } else {
     StageArgs<double> a{};
     a.Us = Uin;
     a.Q = m.Q;
     a.Tu = Tu_in;
     a.Tq = m.Tq;
+    a.Fm = m.Fm;
     a.Un = m.Un;
     a.Uacc = m.Uacc;
     a.Unext = stage < 3 ? m.Us : nullptr;
@@ -190,7 +192,7 @@ size_t smem_bytes(int BD) {
   size_t mx = 0;
   for (int N = 3; N <= 5; ++N) {
     const size_t E = tile_epc(N, BD), n = (size_t)N * N * N, nf = (size_t)N * N;
-    mx = std::max(mx, sizeof(double) * E * (kNS * n + kNQ * n + 6 * kNS * nf + n));
+    mx = std::max(mx, sizeof(double) * E * (kNS * n + kNQ * n + 9 * kNS * nf + n));
     mx = std::max(mx, sizeof(double) * E * (kNQ * n + 6 * kNS * nf));
   }
   return mx;
@@ -404,8 +406,8 @@ int ldg_ensemble_create(const ldg_config* cfgs, int count, ldg_ensemble** out) {
     const size_t nE = pb.nE, n = pb.n, nf = pb.nf;
     void* p[9];
     const size_t sizes[9] = {nE * kNS * n, nE * kNS * n, nE * kNS * n, nE * kNQ * n, nE * 3 * kNQ * nf,
-                             nE * 6 * kNS * nf, nE * 6 * kNS * nf, nE * 2, 0};
-    for (int k = 0; k < 8; ++k)
+                             nE * 6 * kNS * nf, nE * 6 * kNS * nf, nE * 2, nE * 3 * kNS * nf};
+    for (int k = 0; k < 9; ++k)
       if ((st = ens_alloc(e, &p[k], sizes[k] * sizeof(double)))) return bail(st);
     m.Un = (double*)p[0];
     m.Uacc = (double*)p[1];
@@ -415,6 +417,7 @@ int ldg_ensemble_create(const ldg_config* cfgs, int count, ldg_ensemble** out) {
     m.Tu[0] = (double*)p[5];
     m.Tu[1] = (double*)p[6];
     m.diag = (double*)p[7];
+    m.Fm = (double*)p[8];
     max_state = std::max(max_state, nE * kNS * n);
     e->members.push_back(m);
   }

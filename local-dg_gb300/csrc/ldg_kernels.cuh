@@ -166,7 +166,8 @@ template <int N, class T, int E = DefEPC<N>::value>
 __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict__ U,
                                           const typename Real<T>::S* __restrict__ Tu,
                                           typename Real<T>::S* __restrict__ Q,
-                                          typename Real<T>::S* __restrict__ Tq, double* __restrict__ ens,
+                                          typename Real<T>::S* __restrict__ Tq,
+                                          typename Real<T>::S* __restrict__ Fm, double* __restrict__ ens,
                                           const DevOps& ops, const OpsT<T>& o, long e0, int ne,
                                           double* smem_raw) {
   constexpr int n = Cfg<N, E>::n, nf = Cfg<N, E>::nf, EPC = Cfg<N, E>::EPC, NT = Cfg<N, E>::T;
@@ -175,7 +176,8 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
   T* sQ = sU + EPC * kNS * n;              // EPC*15*n
   T* sTp = sQ + EPC * kNQ * n;             // EPC*3*5*nf  own +l traces
   T* sTm = sTp + EPC * 3 * kNS * nf;       // EPC*3*5*nf  (-l neighbour)'s +l traces
-  double* sE = reinterpret_cast<double*>(sTm + EPC * 3 * kNS * nf);  // EPC*n enstrophy
+  T* sTo = sTm + EPC * 3 * kNS * nf;       // EPC*3*5*nf  own -l traces
+  double* sE = reinterpret_cast<double*>(sTo + EPC * 3 * kNS * nf);  // EPC*n enstrophy
   for (int i = threadIdx.x; i < ne * kNS * n; i += NT) sU[i] = R::ld(U + e0 * kNS * n + i);
   for (int i = threadIdx.x; i < ne * 3 * kNS * nf; i += NT) {
     int es = i / (3 * kNS * nf);
@@ -186,8 +188,28 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
     int en = face_neighbour((int)e, 2 * l, ops.nx, ops.ny, ops.nz);
     sTp[i] = R::ld(Tu + (e * 6 + 2 * l + 1) * kNS * nf + r2);
     sTm[i] = R::ld(Tu + ((long)en * 6 + 2 * l + 1) * kNS * nf + r2);
+    sTo[i] = R::ld(Tu + (e * 6 + 2 * l) * kNS * nf + r2);
   }
   __syncthreads();
+  // Roe flux on the three minus faces (numericalFluxC, solver.cpp:1194-1374):
+  // each face is computed once, here, by the element on its plus side; the
+  // element on the minus side uses its negation (the flux is antisymmetric).
+  for (int i = threadIdx.x; i < ne * 3 * nf; i += NT) {
+    const int es2 = i / (3 * nf);
+    const int r = i - es2 * 3 * nf;
+    const int l = r / nf, t = r - l * nf;
+    T uK[kNS], uN[kNS], F[kNS];
+#pragma unroll
+    for (int v = 0; v < kNS; ++v) {
+      uK[v] = sTo[((es2 * 3 + l) * kNS + v) * nf + t];
+      uN[v] = sTm[((es2 * 3 + l) * kNS + v) * nf + t];
+    }
+    if (l == 0) roe_flux<0>(uN, uK, false, o, F);
+    else if (l == 1) roe_flux<1>(uN, uK, false, o, F);
+    else roe_flux<2>(uN, uK, false, o, F);
+#pragma unroll
+    for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + v * nf + t, F[v]);
+  }
   const int es = threadIdx.x / n, q = threadIdx.x % n;
   if (es < ne) {
     const int c[3] = {q % N, (q / N) % N, q / (N * N)};
@@ -200,8 +222,8 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
       const int t = tangential<N>(l, c[0], c[1], c[2]);
       T row[N];
 #pragma unroll
-      for (int r = 0; r < N; ++r) row[r] = o.A[qn * N + r];
-      const T lp = o.Lp[qn], lm = o.Lm[qn], ia = o.ia[l];
+      for (int r = 0; r < N; ++r) row[r] = o.As[l][qn * N + r];
+      const T lp = o.Lps[l][qn], lm = o.Lms[l][qn];
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
         const T* line = sU + (es * kNS + v) * n + b;
@@ -210,7 +232,7 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
         for (int r = 0; r < N; ++r) acc = fma(row[r], line[r * st], acc);
         const T tp = sTp[((es * 3 + l) * kNS + v) * nf + t];
         const T tm = sTm[((es * 3 + l) * kNS + v) * nf + t];
-        const T g = (lp * tp - lm * tm - acc) * ia;
+        const T g = lp * tp - lm * tm - acc;
         grad[l * kNS + v] = g;
         sQ[(es * kNQ + l * kNS + v) * n + q] = g;
         R::st(Q + ((e0 + es) * kNQ + l * kNS + v) * n + q, g);
@@ -262,13 +284,14 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_grad(const typename Real<T>::S* _
                                                     const typename Real<T>::S* __restrict__ Tu,
                                                     typename Real<T>::S* __restrict__ Q,
                                                     typename Real<T>::S* __restrict__ Tq,
+                                                    typename Real<T>::S* __restrict__ Fm,
                                                     double* __restrict__ ens,
                                                     const __grid_constant__ DevOps ops,
                                                     const __grid_constant__ OpsT<T> o) {
   extern __shared__ double smem_raw[];
   const long e0 = (long)blockIdx.x * Cfg<N>::EPC;
   const int ne = (int)min((long)Cfg<N>::EPC, ops.nE - e0);
-  grad_body<N, T>(U, Tu, Q, Tq, ens, ops, o, e0, ne, smem_raw);
+  grad_body<N, T>(U, Tu, Q, Tq, Fm, ens, ops, o, e0, ne, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -350,6 +373,7 @@ struct StageArgs {
   const S* Q;         // its gradient
   const S* Tu;        // its face traces
   const S* Tq;        // gradient minus-face traces
+  const S* Fm;        // Roe fluxes on the minus faces (from the gradient pass)
   const double* Un;   // state at the start of the step
   double* Uacc;       // RK accumulator (u += dt b_s k_s)
   S* Unext;           // next stage input (u + dt a_s k_s); on the last stage
@@ -373,20 +397,19 @@ __device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& o
   using R = Real<T>;
   const bool plus = f & 1;
   const long en = face_neighbour((int)e, f, ops.nx, ops.ny, ops.nz);
-  T uK[kNS], uN[kNS], Du[kNQ];
+  T uK[kNS], Du[kNQ], Fc[kNS], Fv[kNS];
   const auto* tK = a.Tu + (e * 6 + f) * kNS * nf + t;
-  const auto* tN = a.Tu + (en * 6 + (f ^ 1)) * kNS * nf + t;
 #pragma unroll
-  for (int v = 0; v < kNS; ++v) {
-    uK[v] = R::ld(tK + v * nf);
-    uN[v] = R::ld(tN + v * nf);
-  }
+  for (int v = 0; v < kNS; ++v) uK[v] = R::ld(tK + v * nf);
+  // Roe flux: own minus face, or the negated minus-face flux of the plus
+  // neighbour
+  const auto* fm = a.Fm + ((plus ? en : e) * 3 + L) * kNS * nf + t;
+#pragma unroll
+  for (int v = 0; v < kNS; ++v) Fc[v] = sgn(!plus, R::ld(fm + v * nf));
   // q from the element on the plus side (numericalFluxV kWins switch)
   const auto* tq = a.Tq + ((plus ? en : e) * 3 + L) * kNQ * nf + t;
 #pragma unroll
   for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(tq + k * nf);
-  T Fc[kNS], Fv[kNS];
-  roe_flux<L>(uN, uK, plus, o, Fc);
   ViscPre<T> P;
   visc_pre(uK, Du, P);
   visc_column<L>(P, o, Fv);
@@ -418,13 +441,13 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
     visc_pre(u, Du, P);
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
-      T Fc[kNS], Fv[kNS];
-      euler_column(u, es_, l, Fc);
-      if (l == 0) visc_column<0>(P, o, Fv);
-      else if (l == 1) visc_column<1>(P, o, Fv);
-      else visc_column<2>(P, o, Fv);
+      T F[kNS];
+      euler_column(u, es_, l, F);
+      if (l == 0) sub_visc_column<0>(P, o, F);
+      else if (l == 1) sub_visc_column<1>(P, o, F);
+      else sub_visc_column<2>(P, o, F);
 #pragma unroll
-      for (int v = 0; v < kNS; ++v) sF[(es * kNQ + l * kNS + v) * n + q] = Fc[v] - Fv[v];
+      for (int v = 0; v < kNS; ++v) sF[(es * kNQ + l * kNS + v) * n + q] = F[v];
     }
   }
   // 2. numerical fluxes at the face points
@@ -451,11 +474,10 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
       const int st = stride_of<N>(l);
       const int b = q - qn * st;
       const int t = tangential<N>(l, c[0], c[1], c[2]);
-      const T ia = o.ia[l];
       T row[N];
 #pragma unroll
-      for (int r = 0; r < N; ++r) row[r] = o.A[qn * N + r] * ia;
-      const T lp = -(o.Lp[qn] * ia), lm = -(o.Lm[qn] * ia);
+      for (int r = 0; r < N; ++r) row[r] = o.As[l][qn * N + r];
+      const T lp = -o.Lps[l][qn], lm = -o.Lms[l][qn];
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
         const T* line = sF + (es * kNQ + l * kNS + v) * n + b;

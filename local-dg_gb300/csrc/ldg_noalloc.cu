@@ -74,9 +74,10 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   double* Tu = U + ne * kNS * C::n;          // [nE][6][5][nf] face traces of U
   double* Q = Tu + ne * 6 * kNS * C::nf;     // [nE][15][n]   gradient
   double* Tq = Q + ne * kNQ * C::n;          // [nE][3][15][nf] gradient minus-face traces
+  double* Fm = Tq + ne * 3 * kNQ * C::nf;    // [nE][3][5][nf] minus-face Roe fluxes
   const size_t sm_tr = sizeof(double) * 2 * C::EPC * kNS * C::n;
   const size_t sm_trc = sizeof(double) * C::EPC * kNS * C::n;
-  const size_t sm_g = sizeof(double) * C::EPC * (kNS * C::n + kNQ * C::n + 6 * kNS * C::nf + C::n);
+  const size_t sm_g = sizeof(double) * C::EPC * (kNS * C::n + kNQ * C::n + 9 * kNS * C::nf + C::n);
   const size_t sm_r = sizeof(double) * C::EPC * (kNQ * C::n + 6 * kNS * C::nf);
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(k_transform<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tr)) ||
@@ -87,13 +88,14 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   const int grid = (nE + C::EPC - 1) / C::EPC;
   k_transform<N><<<grid, C::T, sm_tr, st>>>(u, U, nE, kNS, ops, 0);
   k_traces<N, double><<<grid, C::T, sm_trc, st>>>(U, nullptr, Tu, nE, o);
-  k_grad<N, double><<<grid, C::T, sm_g, st>>>(U, Tu, Q, Tq, nullptr, ops, o);
+  k_grad<N, double><<<grid, C::T, sm_g, st>>>(U, Tu, Q, Tq, Fm, nullptr, ops, o);
   StageArgs<double> a{};
   std::memset(&a, 0, sizeof(a));
   a.Us = U;
   a.Q = Q;
   a.Tu = Tu;
   a.Tq = Tq;
+  a.Fm = Fm;
   a.Kout = U;  // each thread overwrites only the Gauss point it alone read
   a.stage = -1;
   k_rhs<N, double><<<grid, C::T, sm_r, st>>>(a, ops, o);
@@ -119,7 +121,7 @@ extern "C" int ldg_rhs_noalloc(const ldg_config* cfg, const double* u, double* k
   if (c.device < 0 || c.device >= kMaxDevices) return fail(LDG_ERR_INVALID, "ldg_rhs_noalloc: bad device");
   const int N = c.p + 1, n = N * N * N, nf = N * N;
   const long long nE = (long long)c.nx * c.ny * c.nz;
-  const long long need = nE * (long long)(kNS * n + 6 * kNS * nf + kNQ * n + 3 * kNQ * nf);
+  const long long need = nE * (long long)(kNS * n + 6 * kNS * nf + kNQ * n + 3 * kNQ * nf + 3 * kNS * nf);
   if (need > (long long)kScratchDoubles)
     return fail(LDG_ERR_INVALID,
                 "ldg_rhs_noalloc: mesh needs " + std::to_string(need * 8) + " bytes of scratch; the fixed scratch holds " +
