@@ -47,6 +47,8 @@ extern "C" {
 #define LDG_ERR_UNSUPPORTED -5 /* order or mode not built                  */
 #define LDG_ERR_NODEVICE -6    /* no CUDA device visible                   */
 #define LDG_ERR_TIMEOUT -7     /* a bounded on-device wait gave up          */
+#define LDG_ERR_IO -8          /* a file could not be written or read, or a
+                                  checkpoint failed its checks              */
 
 /* where a pointer lives */
 #define LDG_HOST 0
@@ -155,6 +157,38 @@ int ldg_ke_dissipation(ldg_solver* s, double* eps, int max, int* count);
 
 /* Waits for all work queued on the handle's stream. */
 int ldg_synchronize(ldg_solver* s);
+
+/* ---- Snapshots (solver.cpp:366-381, io.cpp:8-99) and checkpoints. */
+
+/* Writes the current state as the reference's X-Y-Z-V CSV file
+ * (initXYZVFile + exportToXYZVFile, io.cpp:8-72): the header line
+ * "X, Y, Z, u0, u1, u2, u3, u4", then one line per element and node, in
+ * element then node order, holding the node's coordinates (the CGL nodes
+ * mapped into the element, mesh.cpp:389-408) and the five conserved
+ * variables, each printed the way a C++ stream prints a double by default
+ * (printf "%.6g"), separated by ", ".  The file is <filename>.<timeseries>
+ * (io.cpp:30-35), or <filename> when timeseries < 0.  Overwrites. */
+int ldg_write_xyzv(ldg_solver* s, const char* filename, int timeseries);
+
+/* Snapshot cadence of ldg_time_step: with every > 0 it writes
+ * <filename>.<step/every> before each step whose index is a multiple of
+ * every, as dgTimeStep writes output/xyzu.txt.<k> (solver.cpp:366-381).
+ * filename NULL or every <= 0 turns snapshots off (the default). */
+int ldg_set_snapshots(ldg_solver* s, const char* filename, int every);
+
+/* Exact checkpoints.  No reference counterpart: the reference dumps a CSV
+ * of u when it reaches its wall-clock limit (solver.cpp:351-360) and has
+ * no reader.  The file holds the config, the step count and time step,
+ * the internal FP64 Gauss-point state, the face traces of that state and
+ * the KE series, with a 64-bit FNV-1a hash of the payload.  A solver
+ * created from the stored config (ldg_checkpoint_config) that loads the
+ * file continues bit for bit as the saved solver would have.  Loading
+ * into a solver whose discretisation (p, mesh, box, physics, precision or
+ * dt) differs returns LDG_ERR_INVALID; a truncated, foreign or corrupted
+ * file returns LDG_ERR_IO.  Save writes <path>.tmp and renames it. */
+int ldg_save_checkpoint(ldg_solver* s, const char* path);
+int ldg_checkpoint_config(const char* path, ldg_config* cfg);
+int ldg_load_checkpoint(ldg_solver* s, const char* path);
 
 /* The handle's CUDA stream (a cudaStream_t) so callers can order their
  * own work against it. */

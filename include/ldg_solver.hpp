@@ -10,9 +10,11 @@
 // Differences by design: errors throw ldg_gb300::Error instead of exit(-1)
 // (mesh.cpp:102-107, solver.cpp:356-380); the Mesh is a value (the
 // reference's Mesh copy is a non-owning view, array.h:93-99); the MPI
-// decomposition argument is absent (one GPU, periodic wrap on device); CSV
-// snapshots are not written.  Extra accessors expose the state and the
-// kinetic-energy series that dgTimeStep prints (solver.cpp:428-450).
+// decomposition argument is absent (one GPU, periodic wrap on device); the
+// CSV snapshots of dgTimeStep (output/xyzu.txt.<k> every dtSnaps steps,
+// solver.cpp:366-381) are written only after enableSnapshots().  Extra
+// accessors expose the state and the kinetic-energy series that dgTimeStep
+// prints (solver.cpp:428-450), and exact checkpoints.
 #pragma once
 #include <cmath>
 #include <stdexcept>
@@ -91,6 +93,7 @@ class Solver {
     c.box_hi[1] = mesh.topRight().y;
     c.box_hi[2] = mesh.topRight().z;
     c.device = device;
+    dtSnaps_ = dtSnaps;
     check(ldg_create(&c, &s_), "Solver");
   }
   ~Solver() { ldg_destroy(s_); }
@@ -144,10 +147,24 @@ class Solver {
     if (n) check(ldg_ke_dissipation(s_, e.data(), n, &n), "keDissipation");
     return e;
   }
+  // The reference's snapshots: dgTimeStep writes <filename>.<k> before step
+  // k*dtSnaps (solver.cpp:366-381, format io.cpp:8-72).
+  void enableSnapshots(const std::string& filename = "output/xyzu.txt") {
+    check(ldg_set_snapshots(s_, filename.c_str(), dtSnaps_), "enableSnapshots");
+  }
+  void disableSnapshots() { check(ldg_set_snapshots(s_, nullptr, 0), "disableSnapshots"); }
+  // One X-Y-Z-V snapshot of the current state (exportToXYZVFile).
+  void writeSnapshot(const std::string& filename, int timeseries = -1) {
+    check(ldg_write_xyzv(s_, filename.c_str(), timeseries), "writeSnapshot");
+  }
+  // Exact checkpoint / resume (loading requires the same discretisation).
+  void saveCheckpoint(const std::string& path) { check(ldg_save_checkpoint(s_, path.c_str()), "saveCheckpoint"); }
+  void loadCheckpoint(const std::string& path) { check(ldg_load_checkpoint(s_, path.c_str()), "loadCheckpoint"); }
   ldg_solver* handle() { return s_; }
 
  private:
   Mesh mesh_;
+  int dtSnaps_ = 0;
   ldg_solver* s_ = nullptr;
 };
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -15,6 +16,7 @@
 #include "ldg_ops.hpp"
 #include "ldg_problem.hpp"
 #include "ldg_closure.hpp"
+#include "ldg_io.hpp"
 
 using namespace ldg;
 
@@ -77,6 +79,9 @@ struct ldg_solver {
   size_t ev_used = 0;
   double kt_ms[LDG_KERNEL_CLASSES] = {0, 0, 0};
   long long kt_n[LDG_KERNEL_CLASSES] = {0, 0, 0};
+  // snapshot cadence of ldg_time_step (ldg_set_snapshots)
+  std::string snap_file;
+  int snap_every = 0;
 };
 
 namespace {
@@ -627,6 +632,75 @@ int solver_set_gauss_state(ldg_solver* s, const double* U) {
 
 }  // namespace ldg
 
+// ---------------------------------------------------------------- geometry + checkpoints
+namespace ldg {
+
+int solver_geometry(const ldg_solver* s, Geometry* g) {
+  static_assert(kMaxN <= 8, "Geometry holds 8 reference nodes");
+  g->N = s->N;
+  g->nx = s->cfg.nx;
+  g->ny = s->cfg.ny;
+  g->nz = s->cfg.nz;
+  for (int l = 0; l < 3; ++l) {
+    g->lo[l] = s->lo[l];
+    g->hi[l] = s->hi[l];
+  }
+  for (int i = 0; i < kMaxN; ++i) g->xi[i] = s->xi[i];
+  return LDG_OK;
+}
+
+}  // namespace ldg
+
+namespace {
+
+// Checkpoint file: this header, then the FP64 Gauss-point state Un
+// [nE][5][n], the face traces of Un [nE][6][5][nf] (FP64 on the FP64 path,
+// FP32 pairs on the mixed path: 8 bytes per value either way) and the KE
+// series [step].  Native byte order.
+struct CkptHeader {
+  char magic[8];
+  uint32_t version, header_bytes;
+  ldg_config cfg;
+  int64_t step;
+  double dt;
+  int32_t N, nE, precision, pad;
+  int64_t state_bytes, trace_bytes, ke_count;
+  uint64_t payload_hash;
+};
+const char kCkptMagic[8] = {'L', 'D', 'G', 'C', 'K', 'P', 'T', '1'};
+const uint64_t kFnvBasis = 14695981039346656037ull;
+
+// 64-bit FNV-1a (Fowler, Noll, Vo).
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+size_t trace_count(const ldg_solver* s) { return (size_t)s->nE * 6 * kNS * s->nf; }
+
+int read_header(FILE* f, const char* path, CkptHeader* h) {
+  if (std::fread(h, sizeof(*h), 1, f) != 1 || std::memcmp(h->magic, kCkptMagic, 8) != 0 || h->version != 1 ||
+      h->header_bytes != sizeof(CkptHeader))
+    return fail(LDG_ERR_IO, std::string("not a checkpoint of this library: ") + path);
+  return LDG_OK;
+}
+
+// Fields that define the discretisation and must agree for a resume.
+bool same_problem(const ldg_config& a, const ldg_config& b) {
+  bool same = a.p == b.p && a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.L == b.L && a.Re == b.Re &&
+              a.Pr == b.Pr && a.gamma == b.gamma && a.Ma == b.Ma && a.precision == b.precision &&
+              a.use_box == b.use_box;
+  if (same && a.use_box)
+    for (int l = 0; l < 3; ++l) same = same && a.box_lo[l] == b.box_lo[l] && a.box_hi[l] == b.box_hi[l];
+  return same;
+}
+
+}  // namespace
+
 extern "C" {
 
 int ldg_solver_attach_closure(ldg_solver* s, ldg_closure* c) {
@@ -663,6 +737,7 @@ const char* ldg_error_string(int status) {
     case LDG_ERR_UNSUPPORTED: return "LDG_ERR_UNSUPPORTED";
     case LDG_ERR_NODEVICE: return "LDG_ERR_NODEVICE";
     case LDG_ERR_TIMEOUT: return "LDG_ERR_TIMEOUT";
+    case LDG_ERR_IO: return "LDG_ERR_IO";
   }
   return "LDG_ERR_UNKNOWN";
 }
@@ -929,14 +1004,34 @@ int ldg_step(ldg_solver* s, int nsteps) {
 
 int ldg_time_step(ldg_solver* s) {
   if (!s) return fail(LDG_ERR_INVALID, "null solver");
-  long long left = s->timesteps - s->step;
-  while (left > 0) {
+  const long long every = s->snap_every;
+  while (s->step < s->timesteps) {
+    long long left = s->timesteps - s->step;
+    if (every > 0) {
+      // snapshot <file>.<k> before step k*every (solver.cpp:366-381)
+      if (s->step % every == 0) {
+        int st = ldg_write_xyzv(s, s->snap_file.c_str(), (int)(s->step / every));
+        if (st) return st;
+      }
+      left = std::min(left, every - s->step % every);
+    }
     int chunk = (int)std::min<long long>(left, 1 << 20);
     int st = ldg_step(s, chunk);
     if (st) return st;
-    left -= chunk;
   }
   return ldg_synchronize(s);
+}
+
+int ldg_set_snapshots(ldg_solver* s, const char* filename, int every) {
+  if (!s) return fail(LDG_ERR_INVALID, "null solver");
+  if (!filename || !*filename || every <= 0) {
+    s->snap_file.clear();
+    s->snap_every = 0;
+    return LDG_OK;
+  }
+  s->snap_file = filename;
+  s->snap_every = every;
+  return LDG_OK;
 }
 
 int ldg_diagnostics(ldg_solver* s, double* ke_ref, double* ke, double* enstrophy) {
@@ -1045,6 +1140,106 @@ int ldg_probe_fp64_peak(int device, double* tflops) {
   if (err != cudaSuccess) return fail(LDG_ERR_CUDA, cudaGetErrorString(err));
   const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
   *tflops = flops / (ms * 1e-3) / 1e12;
+  return LDG_OK;
+}
+
+int ldg_save_checkpoint(ldg_solver* s, const char* path) {
+  if (!s || !path || !*path) return fail(LDG_ERR_INVALID, "ldg_save_checkpoint: null solver or empty path");
+  LDG_CUDA(cudaSetDevice(s->cfg.device));
+  const size_t ns = state_count(s), nt = trace_count(s), nk = (size_t)s->step;
+  std::vector<double> U(ns), T(nt), ke(nk);
+  LDG_CUDA(cudaMemcpyAsync(U.data(), s->Un, ns * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  LDG_CUDA(cudaMemcpyAsync(T.data(), s->Tu[s->cur], nt * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  if (nk) LDG_CUDA(cudaMemcpyAsync(ke.data(), s->ke_dev, nk * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  LDG_CUDA(cudaStreamSynchronize(s->stream));
+  CkptHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.header_bytes = sizeof(CkptHeader);
+  h.cfg = s->cfg;
+  h.step = s->step;
+  h.dt = s->dt;
+  h.N = s->N;
+  h.nE = s->nE;
+  h.precision = s->mixed ? LDG_MIXED_F32X2 : LDG_FP64;
+  h.state_bytes = (int64_t)(ns * sizeof(double));
+  h.trace_bytes = (int64_t)(nt * sizeof(double));
+  h.ke_count = (int64_t)nk;
+  uint64_t hash = fnv1a(kFnvBasis, U.data(), ns * sizeof(double));
+  hash = fnv1a(hash, T.data(), nt * sizeof(double));
+  h.payload_hash = fnv1a(hash, ke.data(), nk * sizeof(double));
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return fail(LDG_ERR_IO, "cannot open " + tmp + " for writing");
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(U.data(), sizeof(double), ns, f) == ns &&
+            std::fwrite(T.data(), sizeof(double), nt, f) == nt &&
+            (nk == 0 || std::fwrite(ke.data(), sizeof(double), nk, f) == nk);
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) {
+    std::remove(tmp.c_str());
+    return fail(LDG_ERR_IO, "short write to " + tmp);
+  }
+  if (std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    return fail(LDG_ERR_IO, std::string("cannot rename ") + tmp + " to " + path);
+  }
+  return LDG_OK;
+}
+
+int ldg_checkpoint_config(const char* path, ldg_config* cfg) {
+  if (!path || !cfg) return fail(LDG_ERR_INVALID, "ldg_checkpoint_config: null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(LDG_ERR_IO, std::string("cannot open ") + path);
+  CkptHeader h;
+  int st = read_header(f, path, &h);
+  std::fclose(f);
+  if (st) return st;
+  *cfg = h.cfg;
+  return LDG_OK;
+}
+
+int ldg_load_checkpoint(ldg_solver* s, const char* path) {
+  if (!s || !path) return fail(LDG_ERR_INVALID, "ldg_load_checkpoint: null argument");
+  LDG_CUDA(cudaSetDevice(s->cfg.device));
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(LDG_ERR_IO, std::string("cannot open ") + path);
+  CkptHeader h;
+  int st = read_header(f, path, &h);
+  if (st) {
+    std::fclose(f);
+    return st;
+  }
+  const size_t ns = state_count(s), nt = trace_count(s);
+  const int prec = s->mixed ? LDG_MIXED_F32X2 : LDG_FP64;
+  if (!same_problem(h.cfg, s->cfg) || h.N != s->N || h.nE != s->nE || h.precision != prec || h.dt != s->dt) {
+    std::fclose(f);
+    return fail(LDG_ERR_INVALID, std::string("checkpoint ") + path +
+                                     " is of another discretisation (order, mesh, box, physics, precision or dt)");
+  }
+  if (h.step < 0 || h.ke_count != h.step || h.state_bytes != (int64_t)(ns * sizeof(double)) ||
+      h.trace_bytes != (int64_t)(nt * sizeof(double))) {
+    std::fclose(f);
+    return fail(LDG_ERR_IO, std::string("inconsistent checkpoint sizes in ") + path);
+  }
+  const size_t nk = (size_t)h.step;
+  std::vector<double> U(ns), T(nt), ke(nk);
+  bool ok = std::fread(U.data(), sizeof(double), ns, f) == ns && std::fread(T.data(), sizeof(double), nt, f) == nt &&
+            (nk == 0 || std::fread(ke.data(), sizeof(double), nk, f) == nk) && std::fgetc(f) == EOF;
+  std::fclose(f);
+  if (!ok) return fail(LDG_ERR_IO, std::string("truncated or oversized checkpoint ") + path);
+  uint64_t hash = fnv1a(kFnvBasis, U.data(), ns * sizeof(double));
+  hash = fnv1a(hash, T.data(), nt * sizeof(double));
+  if (fnv1a(hash, ke.data(), nk * sizeof(double)) != h.payload_hash)
+    return fail(LDG_ERR_IO, std::string("checkpoint payload hash mismatch (corrupted): ") + path);
+  if ((st = ensure_ke_capacity(s, (long long)nk + 1))) return st;
+  LDG_CUDA(cudaMemcpyAsync(s->Un, U.data(), ns * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  if (s->mixed)  // the FP32-pair stage-0 copy of Un (its traces are replaced next)
+    LDG_CUDA(s_traces(s, true, s->Un, s->Us, s->Tu[s->cur]));
+  LDG_CUDA(cudaMemcpyAsync(s->Tu[s->cur], T.data(), nt * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  if (nk) LDG_CUDA(cudaMemcpyAsync(s->ke_dev, ke.data(), nk * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  LDG_CUDA(cudaStreamSynchronize(s->stream));
+  s->step = (long long)nk;
   return LDG_OK;
 }
 

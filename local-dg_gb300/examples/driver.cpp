@@ -2,7 +2,10 @@
 // driver.cpp:20-47 (commented out there) uses Mesh and Solver:
 //   Mesh mesh{nx,nx,nx,botLeft,topRight,mpi}; Solver dgSolver{p,dtSnaps,tf,L,mesh};
 //   dgSolver.dgTimeStep();
-// Usage: driver <nx> <p> <tf>    (prints dt, steps, and the KE series)
+// Usage: driver <nx> <p> <tf> [snapshot_file]
+//   prints dt, steps and the KE series; with snapshot_file, dgTimeStep also
+//   writes the reference's CSV snapshots <snapshot_file>.<k> every dtSnaps
+//   steps (solver.cpp:366-381).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -21,6 +24,7 @@ int main(int argc, char** argv) {
     ldg_gb300::Mesh mesh{nx, nx, nx, botLeft, topRight};
     int dtSnaps = 30;
     ldg_gb300::Solver dgSolver{p, dtSnaps, tf, L, mesh};
+    if (argc > 4) dgSolver.enableSnapshots(argv[4]);
     std::printf("dt %.17g\nsteps %lld\n", dgSolver.dt(), dgSolver.timesteps());
     dgSolver.dgTimeStep();
     std::vector<double> ke = dgSolver.kineticEnergy();

@@ -31,7 +31,7 @@ LIB = os.path.join(HERE, "libldg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
-SOURCES = ["ldg_capi.cu", "ldg_noalloc.cu", "ldg_ensemble.cu", "ldg_closure.cu", "ldg_ops.cpp"]
+SOURCES = ["ldg_capi.cu", "ldg_noalloc.cu", "ldg_ensemble.cu", "ldg_closure.cu", "ldg_ops.cpp", "ldg_io.cpp"]
 
 LDG_OK = 0
 LDG_HOST = 0
@@ -128,6 +128,11 @@ SIGNATURES = {
     "ldg_ke_history": (_i, [_vp, _dp, _i, _ip]),
     "ldg_ke_dissipation": (_i, [_vp, _dp, _i, _ip]),
     "ldg_synchronize": (_i, [_vp]),
+    "ldg_write_xyzv": (_i, [_vp, ctypes.c_char_p, _i]),
+    "ldg_set_snapshots": (_i, [_vp, ctypes.c_char_p, _i]),
+    "ldg_save_checkpoint": (_i, [_vp, ctypes.c_char_p]),
+    "ldg_checkpoint_config": (_i, [ctypes.c_char_p, ctypes.POINTER(LdgConfig)]),
+    "ldg_load_checkpoint": (_i, [_vp, ctypes.c_char_p]),
     "ldg_stream": (_vp, [_vp]),
     "ldg_enable_kernel_timing": (_i, [_vp, _i]),
     "ldg_kernel_times": (_i, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _i, _i]),
@@ -252,14 +257,35 @@ class Solver:
             cfg.use_box = 1
             for l in range(3):
                 cfg.box_lo[l], cfg.box_hi[l] = box[0][l], box[1][l]
+        self._open(cfg)
+
+    def _open(self, cfg: "LdgConfig") -> None:
         h = ctypes.c_void_p()
-        _check(L_.ldg_create(ctypes.byref(cfg), ctypes.byref(h)), "ldg_create")
+        _check(load().ldg_create(ctypes.byref(cfg), ctypes.byref(h)), "ldg_create")
         self._h = h
         self.cfg = cfg
         info = self.info()
-        self.p, self.dofs, self.nE, self.dt = p, info.dofs, info.nelements, info.dt
+        self.p, self.dofs, self.nE, self.dt = cfg.p, info.dofs, info.nelements, info.dt
         self.timesteps = info.timesteps
         self.shape = (self.nE, 5, self.dofs)
+
+    @classmethod
+    def from_config(cls, cfg: "LdgConfig") -> "Solver":
+        """A solver for an ldg_config (e.g. one stored in a checkpoint)."""
+        self = cls.__new__(cls)
+        self._open(cfg)
+        return self
+
+    @classmethod
+    def from_checkpoint(cls, path: str) -> "Solver":
+        """A solver created from a checkpoint's config with its state,
+        step count and KE series loaded (ldg_checkpoint_config +
+        ldg_load_checkpoint)."""
+        cfg = LdgConfig()
+        _check(load().ldg_checkpoint_config(os.fsencode(path), ctypes.byref(cfg)), "ldg_checkpoint_config")
+        self = cls.from_config(cfg)
+        self.load_checkpoint(path)
+        return self
 
     def close(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -345,6 +371,26 @@ class Solver:
 
     def synchronize(self) -> None:
         _check(load().ldg_synchronize(self._h), "ldg_synchronize")
+
+    def write_xyzv(self, filename: str, timeseries: int = -1) -> None:
+        """The reference's X-Y-Z-V CSV snapshot (io.cpp:8-72) of the state,
+        to <filename>.<timeseries> (or <filename> when timeseries < 0)."""
+        _check(load().ldg_write_xyzv(self._h, os.fsencode(filename), timeseries), "ldg_write_xyzv")
+
+    def set_snapshots(self, filename: str | None, every: int | None = None) -> None:
+        """dg_time_step writes <filename>.<k> before step k*every
+        (solver.cpp:366-381); every defaults to dt_snaps.  None: off."""
+        every = self.cfg.dt_snaps if every is None else every
+        name = os.fsencode(filename) if filename else None
+        _check(load().ldg_set_snapshots(self._h, name, every if filename else 0), "ldg_set_snapshots")
+
+    def save_checkpoint(self, path: str) -> None:
+        _check(load().ldg_save_checkpoint(self._h, os.fsencode(path)), "ldg_save_checkpoint")
+
+    def load_checkpoint(self, path: str) -> None:
+        _check(load().ldg_load_checkpoint(self._h, os.fsencode(path)), "ldg_load_checkpoint")
+        info = self.info()
+        self.timesteps = info.timesteps
 
     def attach_closure(self, closure) -> None:
         """Adds the closure's correction to every RK stage (None: plain LDG)."""

@@ -205,3 +205,37 @@ if __name__ == "__main__":
     u = o.initial_condition()
     u, ke = o.step(u, int(sys.argv[3]))
     print(o.dt, ke)
+
+
+def node_coordinates(nx: int, p: int, L: float = 1.0) -> np.ndarray:
+    """Coordinates (nE, 3, dofs) of the CGL nodes of a periodic nx^3 mesh on
+    [-pi L, pi L]^3: element vertices ix*(hi-lo)/nx + lo (mesh.cpp:128-146),
+    nodes lo_e + (xi+1)/2 (hi_e - lo_e) with xi = cos((p-i) pi/p)
+    (dgMath.cpp:41, mesh.cpp:396-407), node i = ix + iy N + iz N^2."""
+    N = p + 1
+    lo, hi = -math.pi * L, math.pi * L
+    xi = np.array([math.cos((p - i) * math.pi / p) for i in range(N)])
+    out = np.zeros((nx ** 3, 3, N ** 3))
+    for k in range(nx ** 3):
+        idx = (k % nx, (k // nx) % nx, k // (nx * nx))
+        for l in range(3):
+            a = idx[l] * (hi - lo) / nx + lo
+            b = (idx[l] + 1) * (hi - lo) / nx + lo
+            for i in range(N ** 3):
+                c = (i % N, (i // N) % N, i // (N * N))
+                out[k, l, i] = a + .5 * (xi[c[l]] + 1.0) * (b - a)
+    return out
+
+
+def xyzv_text(coords: np.ndarray, u: np.ndarray) -> str:
+    """The reference's X-Y-Z-V CSV (initXYZVFile + exportToXYZVFile,
+    io.cpp:8-72) of a state u (nE, 5, dofs): header, then per element and
+    node 'x, y, z, u0, ..., u4', each value as a C++ stream prints a double
+    by default (%.6g)."""
+    lines = ["X, Y, Z, u0, u1, u2, u3, u4"]
+    nE, _, n = u.shape
+    for k in range(nE):
+        for i in range(n):
+            vals = list(coords[k, :, i]) + list(u[k, :, i])
+            lines.append(", ".join("%.6g" % v for v in vals))
+    return "\n".join(lines) + "\n"

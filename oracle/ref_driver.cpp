@@ -19,6 +19,18 @@
  *   rhs  <nx> <p> <state_in|-> <outprefix> [threads]
  *        One rk4Rhs on the given state (or Taylor-Green), istage 0:
  *        writes <outprefix>.k (dofs,5,nE) and <outprefix>.u0.
+ *   series <nx> <p> <steps> <outprefix> <index_file> [threads]
+ *        Taylor-Green -> <steps> RK4 steps, recording after every step the
+ *        KE (<outprefix>.ke), the sum of squares of each conserved
+ *        variable over all nodes and elements (<outprefix>.norms,
+ *        steps x 5) and the state entries at the flat column-major
+ *        indices listed in <index_file> (int64) (<outprefix>.samples,
+ *        steps x count).  For meshes whose full states are too large to
+ *        keep for every step.
+ *   csv  <nx> <p> <steps> <outprefix> [threads]
+ *        Taylor-Green -> <steps> RK4 steps, then the reference's own
+ *        snapshot writer (initXYZVFile + exportToXYZVFile, io.cpp:8-99)
+ *        on the state: <outprefix>.0.
  */
 #include <cmath>
 #include <cstdio>
@@ -75,12 +87,20 @@ int main(int argc, char** argv) {
   MPI_Init(&argc, &argv);
   std::string mode = argv[1];
   const double L = 1.0;
-  if (mode == "step") {
-    if (argc < 6) { std::fprintf(stderr, "step <nx> <p> <steps> <out> [dump_every] [threads] [state_in]\n"); return 1; }
+  if (mode == "step" || mode == "series" || mode == "csv") {
+    const bool series = mode == "series", csv = mode == "csv";
+    if (argc < (series ? 7 : 6)) {
+      std::fprintf(stderr, "step <nx> <p> <steps> <out> [dump_every] [threads] [state_in]\n"
+                           "series <nx> <p> <steps> <out> <index_file> [threads]\n");
+      return 1;
+    }
     int nx = std::atoi(argv[2]), p = std::atoi(argv[3]), steps = std::atoi(argv[4]);
+    // csv with 0 steps writes the initial condition (the solver is built for 1)
+    const int run_steps = steps;
+    if (csv && steps == 0) steps = 1;
     std::string out = argv[5];
-    int dump_every = argc > 6 ? std::atoi(argv[6]) : steps;
-    int threads = argc > 7 ? std::atoi(argv[7]) : 1;
+    int dump_every = (!series && !csv && argc > 6) ? std::atoi(argv[6]) : steps;
+    int threads = csv ? (argc > 6 ? std::atoi(argv[6]) : 1) : (argc > 7 ? std::atoi(argv[7]) : 1);
     scipy_openblas_set_num_threads(threads);
     MPIUtil mpi{};
     double size = M_PI * L;
@@ -91,7 +111,19 @@ int main(int argc, char** argv) {
     Solver s{p, 1 << 30, tf, L, mesh};
     if (s.timesteps != steps) { std::fprintf(stderr, "timesteps %d != %d\n", (int)s.timesteps, steps); return 2; }
     long nU = (long)s.dofs * s.nStates * s.mesh.nElements;
-    if (argc > 8 && std::string(argv[8]) != "-") read_doubles(argv[8], s.u.data(), nU);
+    if (!series && !csv && argc > 8 && std::string(argv[8]) != "-") read_doubles(argv[8], s.u.data(), nU);
+    std::vector<long long> idx;
+    if (series) {
+      FILE* f = std::fopen(argv[6], "rb");
+      if (!f) { std::fprintf(stderr, "cannot open %s\n", argv[6]); return 2; }
+      long long v;
+      while (std::fread(&v, sizeof(v), 1, f) == 1) {
+        if (v < 0 || v >= nU) { std::fprintf(stderr, "index %lld out of range\n", v); return 2; }
+        idx.push_back(v);
+      }
+      std::fclose(f);
+    }
+    std::vector<double> norms, samples;
 
     /* Work arrays exactly as dgTimeStep allocates them (solver.cpp:298-338). */
     int nStages = 4;
@@ -114,10 +146,10 @@ int main(int argc, char** argv) {
     MPI_Request rk4Reqs[2 * MPIUtil::N_FACES];
     std::vector<double> kes(steps);
 
-    write_doubles(out + ".u0", s.u.data(), nU);
+    if (!series && !csv) write_doubles(out + ".u0", s.u.data(), nU);
     double ke0 = s.computeKE(uInterp3D);
     auto t0 = std::chrono::high_resolution_clock::now();
-    for (int iStep = 0; iStep < steps; ++iStep) {
+    for (int iStep = 0; iStep < run_steps; ++iStep) {
       for (int istage = 0; istage < nStages; ++istage) {
         s.rk4UpdateCurr(uCurr, diagA, ks, istage);
         s.rk4Rhs(uCurr, uInterp2D, uInterp3D, Dus, DuInterp2D, DuInterp3D, toSend, toRecv, rk4Reqs,
@@ -130,6 +162,17 @@ int main(int argc, char** argv) {
             for (int iN = 0; iN < dofs; ++iN)
               s.u(iN, iS, iK) += s.dt * b(istage) * ks(iN, iS, iK, istage);
       kes[iStep] = s.computeKE(uInterp3D);
+      if (series) {
+        for (int iS = 0; iS < nS; ++iS) {
+          double acc = 0.0;
+          for (int iK = 0; iK < nE; ++iK)
+            for (int iN = 0; iN < dofs; ++iN) acc += s.u(iN, iS, iK) * s.u(iN, iS, iK);
+          norms.push_back(acc);
+        }
+        for (long long j : idx) samples.push_back(s.u.data()[j]);
+        continue;
+      }
+      if (csv) continue;
       if ((iStep + 1) % dump_every == 0 || iStep + 1 == steps) {
         std::ostringstream oss;
         oss << out << ".u" << (iStep + 1);
@@ -139,6 +182,14 @@ int main(int argc, char** argv) {
     auto t1 = std::chrono::high_resolution_clock::now();
     double secs = std::chrono::duration<double>(t1 - t0).count();
     write_doubles(out + ".ke", kes.data(), steps);
+    if (csv && !(initXYZVFile(out, 0, "u", nS) && exportToXYZVFile(out, 0, s.mesh.globalCoords, s.u))) {
+      std::fprintf(stderr, "snapshot writer failed\n");
+      return 2;
+    }
+    if (series) {
+      write_doubles(out + ".norms", norms.data(), (long)norms.size());
+      write_doubles(out + ".samples", samples.data(), (long)samples.size());
+    }
     std::ofstream meta(out + ".meta");
     meta.precision(17);
     meta << "nx " << nx << "\np " << p << "\nsteps " << steps << "\ndt " << s.dt << "\ntf " << s.tf

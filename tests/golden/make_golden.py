@@ -5,7 +5,8 @@ oracle/build_ref.sh with the project's MPI/BLAS shim headers) and stores
 compact .npz fixtures.  Needs the reference checkout, so it runs only where
 that exists; the fixtures it writes are committed and travel everywhere.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # the small fixtures
+    python tests/golden/make_golden.py series     # the large-mesh series
 
 Fixtures (arrays use the reference layout u(node,var,elem) = numpy (nE,5,dofs)):
   tgv_n8_p2.npz     Taylor-Green 8^3 p=2, 100 RK4 steps: ke[100], dt,
@@ -14,9 +15,19 @@ Fixtures (arrays use the reference layout u(node,var,elem) = numpy (nE,5,dofs)):
                     u0, k, q (the gradient Dus, (3,nE,5,dofs)), dt.
   step_n{nx}_p{p}.npz  a few RK4 steps from a seeded perturbed state:
                     u0, u_final, ke, steps, dt.
+  xyzv_n{nx}_p{p}_s{steps}.csv.gz  the reference's own X-Y-Z-V snapshot
+                    writer (io.cpp:8-72) on the Taylor-Green state after
+                    <steps> RK4 steps (gzip of the text file).
+  series_n{nx}_p{p}.npz  Taylor-Green runs at the benchmark meshes (32^3
+                    p=3, 200 steps; 64^3 p=4, 2 steps), whose states are
+                    too large to store per step: after every step the KE,
+                    the per-variable sums of squares (norms, steps x 5) and
+                    the entries at seeded flat indices of the
+                    (dofs,5,nE) column-major state (idx, samples).
 """
 from __future__ import annotations
 
+import gzip
 import os
 import subprocess
 import sys
@@ -50,7 +61,33 @@ def meta(path):
     return out
 
 
+SERIES = [(32, 3, 200, 1024, 32), (64, 4, 2, 4096, 64)]  # nx, p, steps, samples, seed
+
+
+def series(threads: int = 8):
+    """The large-mesh per-step series (about 40 min for 32^3 p=3 and 7 min
+    for 64^3 p=4 on 8 cores)."""
+    if not os.path.exists(oracle.REF_BIN):
+        subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        for nx, p, steps, count, seed in SERIES:
+            nU = (p + 1) ** 3 * 5 * nx ** 3
+            idx = np.sort(np.random.default_rng(seed).choice(nU, count, replace=False)).astype(np.int64)
+            idx.tofile(os.path.join(tmp, "idx"))
+            oracle.run_reference(["series", nx, p, steps, "ser", "idx", threads], tmp)
+            m = meta(os.path.join(tmp, "ser.meta"))
+            np.savez_compressed(os.path.join(HERE, f"series_n{nx}_p{p}.npz"), idx=idx,
+                                ke=np.fromfile(os.path.join(tmp, "ser.ke")),
+                                norms=np.fromfile(os.path.join(tmp, "ser.norms")).reshape(steps, 5),
+                                samples=np.fromfile(os.path.join(tmp, "ser.samples")).reshape(steps, count),
+                                dt=m["dt"], steps=steps, ke0=m["ke0"], seconds=m["seconds"], threads=threads)
+            print(f"series_n{nx}_p{p}: {m['seconds']:.1f} s", flush=True)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "series":
+        series()
+        return
     if not os.path.exists(oracle.REF_BIN):
         subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
     with tempfile.TemporaryDirectory() as tmp:
@@ -84,8 +121,14 @@ def main():
             np.savez_compressed(os.path.join(HERE, f"step_n{nx}_p{p}.npz"), u0=u0, u_final=uf,
                                 ke=np.fromfile(os.path.join(tmp, "s.ke")), steps=steps,
                                 dt=meta(os.path.join(tmp, "s.meta"))["dt"], seed=seed)
+        # The reference's CSV snapshots.
+        for nx, p, steps in [(4, 2, 0), (3, 3, 5)]:
+            oracle.run_reference(["csv", nx, p, steps, "snap", 1], tmp)
+            with open(os.path.join(tmp, "snap.0"), "rb") as f_in, \
+                    open(os.path.join(HERE, f"xyzv_n{nx}_p{p}_s{steps}.csv.gz"), "wb") as f_out:
+                f_out.write(gzip.compress(f_in.read(), mtime=0))
     for f in sorted(os.listdir(HERE)):
-        if f.endswith(".npz"):
+        if f.endswith(".npz") or f.endswith(".gz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 

@@ -49,3 +49,21 @@ def test_driver_dgtimestep_matches_oracle(tmp_path):
     u, ke_ref = o.step(o.initial_condition(), steps)
     assert np.max(np.abs(np.array(ke) - ke_ref) / ke_ref) <= 1e-12
     assert abs(vals["u_0_4_0"] - u[0, 4, 0]) <= 1e-12 * abs(u[0, 4, 0])
+
+
+@pytest.mark.gpu
+def test_driver_writes_reference_snapshots(tmp_path):
+    """dgTimeStep with snapshots on: <file>.0 before the first step, in the
+    reference's CSV format (golden file from the reference's writer)."""
+    import gzip
+    from conftest import GOLDEN
+    exe = build_driver(tmp_path)
+    tf = oracle.tf_for_steps(4, 2, 1.0, 5)
+    snap = str(tmp_path / "xyzu.txt")
+    subprocess.run([str(exe), "4", "2", repr(tf), snap], capture_output=True, text=True, check=True)
+    assert sorted(p.name for p in tmp_path.iterdir() if p.name.startswith("xyzu")) == ["xyzu.txt.0"]
+    with gzip.open(os.path.join(GOLDEN, "xyzv_n4_p2_s0.csv.gz"), "rt") as f:
+        ref = f.read().splitlines()
+    got = (tmp_path / "xyzu.txt.0").read_text().splitlines()
+    assert len(got) == len(ref) and got[0] == ref[0]
+    assert sum(a == b for a, b in zip(got, ref)) >= 0.99 * len(ref)
