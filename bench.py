@@ -144,6 +144,19 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, pg=None) -> float:
+    """The largest of every rank's x (the slowest replica sets the job's
+    time); x itself without a process group.  Works on the nccl backend
+    (CUDA tensor) and on gloo (CPU tensor)."""
+    if pg is None:
+        return x
+    import torch
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_baseline(p: int, seconds_budget: float = 20.0, steps: int | None = None):
     """The oracle on the host cores: bounded sample of the workload."""
     import numpy as np
@@ -234,13 +247,9 @@ def time_steps(s, K, W, dev, pg=None, clocks=False):
     finally:
         if clk:
             clk.__exit__(None, None, None)
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), pg)
     kt = s.kernel_times(reset=True)
     s.enable_kernel_timing(False)
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
     return ms, kt, (clk.summary() if clk else None)
 
 
@@ -333,7 +342,7 @@ def run_ours(args):
         s.set_state(host)
         s.step(1)
         s.get_state(host)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
     assert np.all(np.isfinite(host))
     e2e = {"value": ws * n_per_step * Ke / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes}

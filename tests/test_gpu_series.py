@@ -1,0 +1,95 @@
+"""GPU parity at the benchmark meshes, and the enstrophy diagnostic.
+
+Taylor-Green 32^3 p=3 for 200 RK4 steps and 64^3 p=4 for 2 steps against
+the reference's own run (tests/golden/series_*.npz, made by
+tests/golden/make_golden.py series): after every step the KE series, the
+per-variable sums of squares and a seeded sample of state entries.  Bar:
+relative L2 <= 1e-12 per step on the sample (and relative 1e-12 on the KE
+and on the norms).  The reference computes no enstrophy; the GPU's
+enstrophy functional is pinned against a numpy evaluation on the
+reference's own LDG gradient (Dus) of the golden RHS fixtures, and its time
+series along the 32^3 run is recorded and checked to be smooth.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import ldg
+import oracle
+from conftest import GOLDEN, rel_l2
+
+TOL = 1e-12
+
+
+def load(name):
+    path = os.path.join(GOLDEN, name)
+    if not os.path.exists(path):
+        pytest.skip(f"{name} not generated")
+    return np.load(path)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["series_n32_p3.npz", "series_n64_p4.npz"])
+def test_benchmark_mesh_per_step_parity(name):
+    z = load(name)
+    nx, p = int(name.split("_")[1][1:]), int(name.split("_")[2][1:3])
+    steps = int(z["steps"])
+    idx = z["idx"]
+    worst = 0.0
+    enst = []
+    with ldg.Solver(p, nx, steps=steps) as s:
+        assert s.timesteps == steps
+        assert abs(s.dt - float(z["dt"])) <= 1e-15 * float(z["dt"])
+        u = np.empty(s.shape)
+        for k in range(steps):
+            s.step(1)
+            s.get_state(u)
+            err = rel_l2(u.ravel()[idx], z["samples"][k])
+            worst = max(worst, err)
+            assert err <= TOL, (k + 1, err)
+            norms = np.einsum("evq,evq->v", u, u)
+            assert np.max(np.abs(norms - z["norms"][k]) / z["norms"][k]) <= TOL, k + 1
+            if nx == 32 and (k + 1) % 20 == 0:
+                enst.append(s.diagnostics()[2])
+        ke = s.ke_history()
+    assert np.max(np.abs(ke - z["ke"]) / np.abs(z["ke"])) <= TOL
+    if enst:
+        # enstrophy grows smoothly from 3/8 while the vortex stretches
+        enst = np.asarray(enst)
+        assert np.all(np.isfinite(enst)) and np.all(np.diff(enst) > 0)
+        assert abs(enst[0] - 0.375) < 0.01
+
+
+def enstrophy_numpy(u_nodal, q_nodal, nx, p, L=1.0):
+    """Quadrature of rho |curl v|^2 / 2, normalised by rho0 (2 pi L)^3, from
+    nodal u (nE,5,n) and the LDG gradient q (3,nE,5,n), evaluated at the
+    Gauss points (Interp3D of the reference)."""
+    o = oracle.Oracle(nx, p)
+    n = (p + 1) ** 3
+    I3 = o.operator(1).reshape(n, n, order="F")
+    w3 = o.operator(5)
+    U = np.einsum("qi,evi->evq", I3, u_nodal)
+    Q = np.einsum("qi,levi->levq", I3, q_nodal)
+    rho = U[:, 0]
+    v = U[:, 1:4] / rho[:, None]
+    G = np.empty((3, 3) + rho.shape)  # G[i][j] = d v_i / d x_j
+    for i in range(3):
+        for j in range(3):
+            G[i, j] = (Q[j, :, 1 + i] - Q[j, :, 0] * v[:, i]) / rho
+    wx, wy, wz = G[2, 1] - G[1, 2], G[0, 2] - G[2, 0], G[1, 0] - G[0, 1]
+    J = (np.pi * L / nx) ** 3
+    dens = 0.5 * rho * (wx ** 2 + wy ** 2 + wz ** 2)
+    return float(np.sum(dens * w3[None, :]) * J / (2 * np.pi * L) ** 3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["rhs_n3_p2.npz", "rhs_n4_p3.npz", "rhs_n3_p4.npz"])
+def test_enstrophy_matches_reference_gradient(name):
+    z = load(name)
+    nx, p = int(name.split("_")[1][1:]), int(name.split("_")[2][1])
+    ref = enstrophy_numpy(z["u0"], z["q"], nx, p)
+    with ldg.Solver(p, nx) as s:
+        s.set_state(z["u0"])
+        _, _, ens = s.diagnostics()
+    assert abs(ens - ref) <= TOL * abs(ref), (ens, ref)
