@@ -126,3 +126,20 @@ def test_conservation_of_mass():
     tot = lambda u: np.einsum("evq,q->v", u, c)
     u, _ = o.step(z["u0"], 5)
     assert abs(tot(u)[0] - tot(z["u0"])[0]) <= 1e-13 * abs(tot(z["u0"])[0])
+
+
+def test_oracle_matches_reference_series_at_32_cubed_p3():
+    """The first two steps of the reference's 32^3 p=3 Taylor-Green run
+    (tests/golden/series_n32_p3.npz): KE, per-variable norms and the
+    sampled entries."""
+    z = np.load(os.path.join(GOLDEN, "series_n32_p3.npz"))
+    o = oracle.Oracle(32, 3, steps=int(z["steps"]), threads=os.cpu_count() or 1,
+                      openblas=oracle.find_openblas())
+    assert o.dt == float(z["dt"])
+    u = o.initial_condition()
+    for k in range(2):
+        u, ke = o.step(u, 1)
+        assert abs(ke[0] - z["ke"][k]) <= 1e-12 * z["ke"][k]
+        assert rel_l2(u.ravel()[z["idx"]], z["samples"][k]) <= 1e-12
+        norms = np.einsum("evq,evq->v", u, u)
+        assert np.max(np.abs(norms - z["norms"][k]) / z["norms"][k]) <= 1e-12
