@@ -275,9 +275,15 @@ int ldg_closure_mlp_backward(ldg_closure* c, const float* x, const float* dy, in
 /* Raw samples [first, first+count): features (count x 20 (p+1)^3) and
  * targets (count x 5 (p+1)^3) as float; either pointer may be NULL. */
 int ldg_closure_get_samples(ldg_closure* c, long long first, long long count, float* X, float* Y);
-/* Elements whose correction was dropped (non-finite prediction). */
+/* Element-stage corrections dropped so far (features outside the
+ * training range, |x| > 10 training standard deviations, or a non-finite
+ * prediction: the element keeps the plain LDG operator). */
 int ldg_closure_fallbacks(ldg_closure* c, long long* count);
-/* Attach (c) or detach (NULL) a closure on a coarse FP64 solver. */
+/* The same count, and the element-stage corrections whose kinetic-energy
+ * raising component was removed (energy-stable projection). */
+int ldg_closure_counters(ldg_closure* c, long long* fallbacks, long long* clipped);
+/* Attach (c) or detach (NULL) a closure on a coarse FP64 solver: every RK
+ * stage of ldg_step, and ldg_rhs, then add the closure's correction. */
 int ldg_solver_attach_closure(ldg_solver* s, ldg_closure* c);
 
 /* RHS evaluation without any device allocation.  No counterpart in the

@@ -919,6 +919,11 @@ int ldg_rhs(ldg_solver* s, const double* u_curr, double* k, int where) {
   }
   LDG_CUDA(s_grad(s, s->mixed, Uin, Tu, nullptr));
   StageCall c;
+  if (s->closure) {  // the RHS the RK stages use: plain LDG plus the learned correction
+    st = closure_correction(s->closure, solver_view(s), (const double*)Uin, s->Q, s->Kadd, s->stream);
+    if (st) return st;
+    c.Kadd = s->Kadd;
+  }
   c.Us = Uin;
   c.Q = s->Q;
   c.Tu = Tu;

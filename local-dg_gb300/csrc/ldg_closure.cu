@@ -12,9 +12,18 @@
 // outputs normalised per channel; BF16 weights and activations, FP32
 // accumulation on the tensor cores (ldg_mlp.cuh), FP32 master weights with
 // Adam.  In a coarse solver with the closure attached, every RK stage adds
-// the de-normalised prediction to the RHS before the RK update; elements
-// whose prediction is not finite get no correction (the plain LDG operator)
-// and are counted.
+// the de-normalised prediction to the RHS before the RK update, after two
+// safeguards:
+//   * fallback: an element whose normalised features leave the training
+//     range (|x| > kOodSigma) or whose prediction is not finite gets no
+//     correction (the plain LDG operator); such elements are counted;
+//   * energy stability: the component of the correction that would raise
+//     the element's kinetic energy is removed.  With g_q = dKE/du at Gauss
+//     point q, (-|v|^2/2, v, 0), the rate sum_q w_q g_q . d of a correction
+//     d is made <= 0 by the smallest change in the element's L2 norm,
+//     d <- d - lambda g with lambda = max(0, sum w g.d) / sum w g.g
+//     (an element-wise form of backscatter clipping); clipped elements are
+//     counted.  The correction can then only dissipate kinetic energy.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -174,40 +183,89 @@ __global__ void k_gather_norm(const float* __restrict__ X, const float* __restri
   }
 }
 
-// Features of every element of a solver state for inference.
+// Normalised features beyond this many training standard deviations mark an
+// element as outside the training range.
+constexpr float kOodSigma = 10.f;
+
+// Features of every element of a solver state for inference; ood[e] is set
+// when a feature of element e is outside the training range (or not finite).
 __global__ void k_features(const double* __restrict__ U, const double* __restrict__ Q, int nE, int n,
                            const float* __restrict__ mi, const float* __restrict__ si,
-                           __nv_bfloat16* __restrict__ Xb) {
+                           __nv_bfloat16* __restrict__ Xb, int* __restrict__ ood) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long in_dim = (long)kChIn * n;
   if (i >= (long)nE * in_dim) return;
   const long e = i / in_dim, j = i % in_dim;
   const int c = (int)(j / n);
   const double v = j < 5 * n ? U[e * 5 * n + j] : Q[e * 15 * n + (j - 5 * n)];
-  Xb[i] = __float2bfloat16(((float)v - mi[c]) / si[c]);
+  const float x = ((float)v - mi[c]) / si[c];
+  if (!(fabsf(x) <= kOodSigma)) ood[e] = 1;
+  Xb[i] = __float2bfloat16(x);
 }
 
-// De-normalised correction into the RHS term; a non-finite prediction of an
-// element leaves that element uncorrected (plain LDG) and is counted.
-__global__ void k_correction(const float* __restrict__ Yn, int nE, int n, const float* __restrict__ mo,
-                             const float* __restrict__ so, double* __restrict__ Kadd,
-                             unsigned long long* __restrict__ fallbacks) {
+struct GaussW {
+  double w[8];
+};
+
+// De-normalised, energy-stable correction into the RHS term (one CTA per
+// element, n <= 512 points).  Elements marked out of range or with a
+// non-finite prediction get no correction.
+__global__ void k_correction(const float* __restrict__ Yn, const double* __restrict__ U, int nE, int N,
+                             const float* __restrict__ mo, const float* __restrict__ so, const GaussW gw,
+                             const int* __restrict__ ood, double* __restrict__ Kadd,
+                             unsigned long long* __restrict__ counters) {
   const int e = blockIdx.x;
   if (e >= nE) return;
+  const int n = N * N * N, out_dim = kChOut * n;
   __shared__ int bad;
-  if (threadIdx.x == 0) bad = 0;
+  __shared__ double sp[128], sg[128];
+  if (threadIdx.x == 0) bad = ood[e];
   __syncthreads();
-  const int out_dim = kChOut * n;
-  for (int j = threadIdx.x; j < out_dim; j += blockDim.x) {
-    const float y = Yn[(long)e * out_dim + j];
-    if (!isfinite(y)) bad = 1;
-  }
+  for (int j = threadIdx.x; j < out_dim; j += blockDim.x)
+    if (!isfinite(Yn[(long)e * out_dim + j])) bad = 1;
   __syncthreads();
-  for (int j = threadIdx.x; j < out_dim; j += blockDim.x) {
-    const int c = j / n;
-    Kadd[(long)e * out_dim + j] = bad ? 0.0 : (double)(Yn[(long)e * out_dim + j] * so[c] + mo[c]);
+  if (bad) {
+    for (int j = threadIdx.x; j < out_dim; j += blockDim.x) Kadd[(long)e * out_dim + j] = 0.0;
+    if (threadIdx.x == 0) atomicAdd(&counters[0], 1ULL);
+    return;
   }
-  if (bad && threadIdx.x == 0) atomicAdd(fallbacks, 1ULL);
+  // KE production of the correction, sum_q w_q g_q . d_q, and sum_q w_q |g_q|^2
+  double pr = 0.0, gg = 0.0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const double* u = U + (long)e * 5 * n + q;
+    const double ir = 1.0 / u[0];
+    const double v0 = u[n] * ir, v1 = u[2 * n] * ir, v2 = u[3 * n] * ir;
+    const double g0 = -0.5 * (v0 * v0 + v1 * v1 + v2 * v2);
+    const double w = gw.w[q % N] * gw.w[(q / N) % N] * gw.w[q / (N * N)];
+    double d[4];
+    for (int c = 0; c < 4; ++c) d[c] = (double)(Yn[(long)e * out_dim + c * n + q] * so[c] + mo[c]);
+    pr += w * (g0 * d[0] + v0 * d[1] + v1 * d[2] + v2 * d[3]);
+    gg += w * (g0 * g0 + v0 * v0 + v1 * v1 + v2 * v2);
+  }
+  sp[threadIdx.x] = pr;
+  sg[threadIdx.x] = gg;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {  // fixed-order tree (deterministic)
+    if (threadIdx.x < h) {
+      sp[threadIdx.x] += sp[threadIdx.x + h];
+      sg[threadIdx.x] += sg[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  const double lambda = (sp[0] > 0.0 && sg[0] > 0.0) ? sp[0] / sg[0] : 0.0;
+  for (int j = threadIdx.x; j < out_dim; j += blockDim.x) {
+    const int c = j / n, q = j % n;
+    double d = (double)(Yn[(long)e * out_dim + j] * so[c] + mo[c]);
+    if (lambda > 0.0 && c < 4) {
+      const double* u = U + (long)e * 5 * n + q;
+      const double ir = 1.0 / u[0];
+      const double v0 = u[n] * ir, v1 = u[2 * n] * ir, v2 = u[3 * n] * ir;
+      const double g = c == 0 ? -0.5 * (v0 * v0 + v1 * v1 + v2 * v2) : (c == 1 ? v0 : (c == 2 ? v1 : v2));
+      d -= lambda * g;
+    }
+    Kadd[(long)e * out_dim + j] = d;
+  }
+  if (lambda > 0.0 && threadIdx.x == 0) atomicAdd(&counters[1], 1ULL);
 }
 
 __global__ void k_f2bf(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, long count) {
@@ -265,7 +323,9 @@ struct ldg_closure {
   // projection scratch
   double *pf_K = nullptr, *pc_U = nullptr, *pc_KT = nullptr, *pc_K = nullptr;
   long pf_cap = 0, pc_cap = 0;
-  unsigned long long* fallbacks = nullptr;
+  unsigned long long* fallbacks = nullptr;  // [0] elements left uncorrected, [1] elements clipped
+  int* ood = nullptr;                       // per element: features outside the training range
+  double gw[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // Gauss weights of order p
 };
 
 namespace {
@@ -285,7 +345,7 @@ int ensure_workspace(ldg_closure* c, int B) {
   if (B <= c->wcap) return LDG_OK;
   int cap = std::max(B, 1024);
   void* ptrs[] = {c->Xb, c->H1, c->H2, c->dYb, c->dZ2b, c->dZ1b, c->Z1, c->Z2, c->Yo, c->Tn,
-                  c->dY, c->dH2, c->dZ2, c->dH1, c->dZ1, c->rowl, c->idx, c->evalbuf};
+                  c->dY, c->dH2, c->dZ2, c->dH1, c->dZ1, c->rowl, c->idx, c->evalbuf, c->ood};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   const long H = c->hidden, I = c->in_dim, O = c->out_dim;
@@ -298,7 +358,8 @@ int ensure_workspace(ldg_closure* c, int B) {
       (st = cl_alloc(&c->dY, (size_t)cap * O)) || (st = cl_alloc(&c->dH2, (size_t)cap * H)) ||
       (st = cl_alloc(&c->dZ2, (size_t)cap * H)) || (st = cl_alloc(&c->dH1, (size_t)cap * H)) ||
       (st = cl_alloc(&c->dZ1, (size_t)cap * H)) || (st = cl_alloc(&c->rowl, (size_t)cap)) ||
-      (st = cl_alloc(&c->idx, (size_t)cap)) || (st = cl_alloc(&c->evalbuf, (size_t)cap * 2)))
+      (st = cl_alloc(&c->idx, (size_t)cap)) || (st = cl_alloc(&c->evalbuf, (size_t)cap * 2)) ||
+      (st = cl_alloc(&c->ood, (size_t)cap)))
     return st;
   c->wcap = cap;
   return LDG_OK;
@@ -416,11 +477,16 @@ int closure_correction(ldg_closure* c, const SolverView& v, const double* U, con
   int rc = ensure_workspace(c, v.nE);
   if (!rc) {
     const float* s = c->stats;
-    k_features<<<(unsigned)ceil_div((long)v.nE * c->in_dim, 256), 256, 0, st>>>(U, Q, v.nE, c->n, s, s + 20,
-                                                                                 c->Xb);
-    cudaError_t e = forward(c, v.nE);
+    cudaError_t e = cudaMemsetAsync(c->ood, 0, sizeof(int) * v.nE, st);
     if (e == cudaSuccess) {
-      k_correction<<<v.nE, 128, 0, st>>>(c->Yo, v.nE, c->n, s + 40, s + 45, Kadd, c->fallbacks);
+      k_features<<<(unsigned)ceil_div((long)v.nE * c->in_dim, 256), 256, 0, st>>>(U, Q, v.nE, c->n, s, s + 20,
+                                                                                   c->Xb, c->ood);
+      e = forward(c, v.nE);
+    }
+    if (e == cudaSuccess) {
+      GaussW gw;
+      for (int i = 0; i < 8; ++i) gw.w[i] = c->gw[i];
+      k_correction<<<v.nE, 128, 0, st>>>(c->Yo, U, v.nE, c->N, s + 40, s + 45, gw, c->ood, Kadd, c->fallbacks);
       e = cudaGetLastError();
     }
     if (e != cudaSuccess) rc = fail(LDG_ERR_CUDA, std::string("closure inference: ") + cudaGetErrorString(e));
@@ -445,6 +511,14 @@ int ldg_closure_create(int p, int hidden, unsigned long long seed, int device, l
   c->p = p;
   c->N = p + 1;
   c->n = c->N * c->N * c->N;
+  {
+    Ops1D o1;
+    if (!build_ops1d(p, &o1)) {
+      delete c;
+      return fail(LDG_ERR_UNSUPPORTED, "closure: no Gauss rule for this order");
+    }
+    for (int i = 0; i < c->N; ++i) c->gw[i] = o1.w[i];
+  }
   c->in_dim = kChIn * c->n;
   c->out_dim = kChOut * c->n;
   c->hidden = hidden;
@@ -465,7 +539,7 @@ int ldg_closure_create(int p, int hidden, unsigned long long seed, int device, l
   if ((st = cl_alloc(&c->theta, c->n_params)) || (st = cl_alloc(&c->grad, c->n_params)) ||
       (st = cl_alloc(&c->m, c->n_params)) || (st = cl_alloc(&c->v, c->n_params)) ||
       (st = cl_alloc(&c->wb, c->n_params)) || (st = cl_alloc(&c->stats, 64)) ||
-      (st = cl_alloc(&c->fallbacks, 1))) {
+      (st = cl_alloc(&c->fallbacks, 2))) {
     ldg_closure_destroy(c);
     return st;
   }
@@ -486,7 +560,7 @@ int ldg_closure_create(int p, int hidden, unsigned long long seed, int device, l
   if (cudaMemcpy(c->theta, h.data(), sizeof(float) * c->n_params, cudaMemcpyHostToDevice) ||
       cudaMemset(c->m, 0, sizeof(float) * c->n_params) || cudaMemset(c->v, 0, sizeof(float) * c->n_params) ||
       cudaMemcpy(c->stats, stats.data(), sizeof(float) * 64, cudaMemcpyHostToDevice) ||
-      cudaMemset(c->fallbacks, 0, sizeof(unsigned long long))) {
+      cudaMemset(c->fallbacks, 0, 2 * sizeof(unsigned long long))) {
     ldg_closure_destroy(c);
     return fail(LDG_ERR_CUDA, "closure: initial upload");
   }
@@ -505,7 +579,8 @@ int ldg_closure_destroy(ldg_closure* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* ptrs[] = {c->theta, c->grad, c->m, c->v, c->wb, c->stats, c->X, c->Y, c->Xb, c->H1, c->H2,
                   c->dYb, c->dZ2b, c->dZ1b, c->Z1, c->Z2, c->Yo, c->Tn, c->dY, c->dH2, c->dZ2, c->dH1,
-                  c->dZ1, c->rowl, c->idx, c->evalbuf, c->pf_K, c->pc_U, c->pc_KT, c->pc_K, c->fallbacks};
+                  c->dZ1, c->rowl, c->idx, c->evalbuf, c->pf_K, c->pc_U, c->pc_KT, c->pc_K, c->fallbacks,
+                  c->ood};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -743,10 +818,15 @@ int ldg_closure_get_samples(ldg_closure* c, long long first, long long count, fl
 }
 
 int ldg_closure_fallbacks(ldg_closure* c, long long* count) {
-  if (!c || !count) return fail(LDG_ERR_INVALID, "closure: null argument");
-  unsigned long long h = 0;
-  CL_CUDA(cudaMemcpy(&h, c->fallbacks, sizeof(h), cudaMemcpyDeviceToHost));
-  *count = (long long)h;
+  return ldg_closure_counters(c, count, nullptr);
+}
+
+int ldg_closure_counters(ldg_closure* c, long long* fallbacks, long long* clipped) {
+  if (!c || (!fallbacks && !clipped)) return fail(LDG_ERR_INVALID, "closure: null argument");
+  unsigned long long h[2] = {0, 0};
+  CL_CUDA(cudaMemcpy(h, c->fallbacks, sizeof(h), cudaMemcpyDeviceToHost));
+  if (fallbacks) *fallbacks = (long long)h[0];
+  if (clipped) *clipped = (long long)h[1];
   return LDG_OK;
 }
 

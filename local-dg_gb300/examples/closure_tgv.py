@@ -21,7 +21,10 @@ fine FP64 evaluation run:
   a priori      RHS error on the held-out samples, plain vs closure
   a posteriori  KE-dissipation rate -(dKE/dt) (the reference's
                 keDissipation, solver.cpp:438-440) of the coarse runs with
-                and without the closure, against the fine run, to --t-end
+                and without the closure, against the fine run, to --t-end;
+                the attached closure is energy-stable (its correction never
+                raises an element's kinetic energy) and falls back to plain
+                LDG outside the training range
 
 Writes a JSON summary after each phase (a partial run still reports) and
 the raw KE series to <out>.npz.  Usage:
@@ -147,10 +150,16 @@ def main():
     series["losses"] = losses
     e_plain, e_closure = closure.evaluate(n_train, n_held)
     e_plain_tr, e_closure_tr = closure.evaluate(0, n_train)
+    per = n_held // n_times
+    by_time = []
+    for k in range(n_times):
+        a, b = closure.evaluate(n_train + k * per, per)
+        by_time.append([k * per_sample * dt_eval, a, b])
     res["training"] = {"seconds": time.perf_counter() - t0, "samples": n_train, "params": closure.n_params,
                        "loss_first50": float(np.mean(losses[:50])), "loss_last50": float(np.mean(losses[-50:]))}
     res["a_priori"] = {"heldout_samples": n_held, "rhs_err_plain": e_plain, "rhs_err_closure": e_closure,
                        "train_rhs_err_plain": e_plain_tr, "train_rhs_err_closure": e_closure_tr,
+                       "heldout_by_time": by_time,
                        "units": "mean squared RHS error over the normalised target channels"}
     save()
 
@@ -180,7 +189,8 @@ def main():
     for name in ("plain", "closure"):
         summary[name] = compare(name, series["ke_" + name], res["coarse_runs"][name]["dt"], tf_, ef, scale)
         summary[name]["status"] = res["coarse_runs"][name]["status"]
-    summary["closure_fallback_elements"] = closure.fallbacks
+    summary["closure_fallback_element_stages"] = closure.fallbacks
+    summary["closure_clipped_element_stages"] = closure.clipped
     res["a_posteriori"] = summary
     save()
     closure.close()

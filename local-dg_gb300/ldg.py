@@ -162,6 +162,7 @@ SIGNATURES = {
     "ldg_closure_mlp_backward": (_i, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _i,
                                       ctypes.POINTER(ctypes.c_float)]),
     "ldg_closure_fallbacks": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "ldg_closure_counters": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     "ldg_closure_get_samples": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(ctypes.c_float),
                                      ctypes.POINTER(ctypes.c_float)]),
     "ldg_solver_attach_closure": (_i, [_vp, _vp]),
@@ -538,6 +539,13 @@ class Closure:
         Y = np.zeros((count, self.out_dim), dtype=np.float32)
         _check(load().ldg_closure_get_samples(self._h, first, count, _fp(X), _fp(Y)), "ldg_closure_get_samples")
         return X, Y
+
+    @property
+    def clipped(self) -> int:
+        """Element-stage corrections whose KE-raising part was removed."""
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        _check(load().ldg_closure_counters(self._h, ctypes.byref(a), ctypes.byref(b)), "ldg_closure_counters")
+        return b.value
 
     @property
     def fallbacks(self) -> int:

@@ -120,3 +120,41 @@ def test_closure_end_to_end_reduces_heldout_rhs_error():
             assert c.fallbacks == 0
             a.attach_closure(None)  # detach: plain operator again
             a.step(1)
+
+
+@pytest.mark.gpu
+def test_attached_correction_never_raises_element_kinetic_energy():
+    """Energy stability: with the closure attached, rhs(u) - rhs_plain(u)
+    has, in every element, a kinetic-energy production
+    sum_q w_q (v . dm - |v|^2/2 drho) <= 0 (up to rounding), evaluated here
+    in numpy at the Gauss points (Interp3D of the reference)."""
+    with ldg.Closure(p=2, hidden=64, seed=13) as c:
+        for inst in (0, 1):
+            fine, coarse = fine_coarse_pair(9, inst, 0)
+            with fine, coarse:
+                for _ in range(3):
+                    c.add_samples(fine, coarse)
+                    fine.step(15)
+        c.finalize(0, c.samples)
+        c.train(0, c.samples, iters=200, batch=256, lr=2e-3, seed=1)
+        with ldg.Solver(2, 4, steps=10, perturb_amp=0.05, seed=9, instance=5) as a, \
+                ldg.Solver(2, 4, steps=10, perturb_amp=0.05, seed=9, instance=5) as b:
+            a.step(3)
+            u = a.get_state()
+            k_plain = b.rhs(u)
+            a.attach_closure(c)
+            k_cl = a.rhs(u)
+            clipped = c.clipped
+    o = oracle.Oracle(4, 2)
+    n = 27
+    I3 = o.operator(1).reshape(n, n, order="F")
+    w3 = o.operator(5)
+    U = np.einsum("qi,evi->evq", I3, u)
+    D = np.einsum("qi,evi->evq", I3, k_cl - k_plain)
+    assert np.max(np.abs(D)) > 0  # the closure does act
+    v = U[:, 1:4] / U[:, 0:1]
+    g0 = -0.5 * np.sum(v * v, axis=1)
+    prod = np.sum(w3 * (g0 * D[:, 0] + np.sum(v * D[:, 1:4], axis=1)), axis=1)
+    scale = np.sum(w3 * (np.abs(g0 * D[:, 0]) + np.sum(np.abs(v * D[:, 1:4]), axis=1)), axis=1)
+    assert np.all(prod <= 1e-10 * scale + 1e-300), prod.max()
+    assert clipped >= 0

@@ -62,8 +62,7 @@ def test_driver_writes_reference_snapshots(tmp_path):
     snap = str(tmp_path / "xyzu.txt")
     subprocess.run([str(exe), "4", "2", repr(tf), snap], capture_output=True, text=True, check=True)
     assert sorted(p.name for p in tmp_path.iterdir() if p.name.startswith("xyzu")) == ["xyzu.txt.0"]
+    from test_io import assert_same_csv
     with gzip.open(os.path.join(GOLDEN, "xyzv_n4_p2_s0.csv.gz"), "rt") as f:
-        ref = f.read().splitlines()
-    got = (tmp_path / "xyzu.txt.0").read_text().splitlines()
-    assert len(got) == len(ref) and got[0] == ref[0]
-    assert sum(a == b for a, b in zip(got, ref)) >= 0.99 * len(ref)
+        ref = f.read()
+    assert_same_csv((tmp_path / "xyzu.txt.0").read_text(), ref)
