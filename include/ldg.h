@@ -265,6 +265,8 @@ int ldg_closure_train(ldg_closure* c, long long first, long long count, int iter
 int ldg_closure_evaluate(ldg_closure* c, long long first, long long count, double* err_plain, double* err_closure);
 int ldg_closure_param_count(const ldg_closure* c, long long* count);
 int ldg_closure_get_params(ldg_closure* c, float* out);
+/* Sets the parameters (layout of ldg_closure_get_params) and restarts the
+ * optimiser (Adam moments and step count). */
 int ldg_closure_set_params(ldg_closure* c, const float* in);
 /* mean[20], std[20] of the input channels, mean[5], std[5] of the outputs */
 int ldg_closure_get_stats(ldg_closure* c, float* out50);
@@ -276,12 +278,37 @@ int ldg_closure_mlp_backward(ldg_closure* c, const float* x, const float* dy, in
  * targets (count x 5 (p+1)^3) as float; either pointer may be NULL. */
 int ldg_closure_get_samples(ldg_closure* c, long long first, long long count, float* X, float* Y);
 /* Element-stage corrections dropped so far (features outside the
- * training range, |x| > 10 training standard deviations, or a non-finite
+ * training range, |x| > ood_sigma training standard deviations, or a non-finite
  * prediction: the element keeps the plain LDG operator). */
 int ldg_closure_fallbacks(ldg_closure* c, long long* count);
 /* The same count, and the element-stage corrections whose kinetic-energy
  * raising component was removed (energy-stable projection). */
 int ldg_closure_counters(ldg_closure* c, long long* fallbacks, long long* clipped);
+/* Training and inference options.
+ *   input_noise  standard deviation of Gaussian noise added to the
+ *                normalised features of every training batch (0: none)
+ *   energy       what the attached correction may do to an element's
+ *                kinetic energy: LDG_CLOSURE_ENERGY_NONE (no constraint),
+ *                _DISSIPATIVE (its KE-raising component is removed; the
+ *                default), _NEUTRAL (its KE production is removed)
+ *   scale        factor on the correction before the projection (1)
+ *   ood_sigma    elements with a normalised feature beyond this many
+ *                training standard deviations keep the plain LDG RHS (10)
+ *   lr_final     cosine decay of the learning rate from lr to
+ *                lr * lr_final over a training call (1: constant) */
+#define LDG_CLOSURE_ENERGY_NONE 0
+#define LDG_CLOSURE_ENERGY_DISSIPATIVE 1
+#define LDG_CLOSURE_ENERGY_NEUTRAL 2
+typedef struct ldg_closure_options {
+  float input_noise;
+  int energy;
+  float scale;
+  float ood_sigma;
+  float lr_final;
+  int reserved[3];
+} ldg_closure_options;
+int ldg_closure_get_options(const ldg_closure* c, ldg_closure_options* o);
+int ldg_closure_set_options(ldg_closure* c, const ldg_closure_options* o);
 /* Attach (c) or detach (NULL) a closure on a coarse FP64 solver: every RK
  * stage of ldg_step, and ldg_rhs, then add the closure's correction. */
 int ldg_solver_attach_closure(ldg_solver* s, ldg_closure* c);

@@ -15,15 +15,21 @@
 // the de-normalised prediction to the RHS before the RK update, after two
 // safeguards:
 //   * fallback: an element whose normalised features leave the training
-//     range (|x| > kOodSigma) or whose prediction is not finite gets no
-//     correction (the plain LDG operator); such elements are counted;
-//   * energy stability: the component of the correction that would raise
-//     the element's kinetic energy is removed.  With g_q = dKE/du at Gauss
-//     point q, (-|v|^2/2, v, 0), the rate sum_q w_q g_q . d of a correction
-//     d is made <= 0 by the smallest change in the element's L2 norm,
+//     range (|x| > ood_sigma, 10 by default) or whose prediction is not
+//     finite gets no correction (the plain LDG operator); such elements are
+//     counted;
+//   * energy stability (option `energy`, dissipative by default): the
+//     component of the correction that would raise the element's kinetic
+//     energy is removed.  With g_q = dKE/du at Gauss point q,
+//     (-|v|^2/2, v, 0), the rate sum_q w_q g_q . d of a correction d is made
+//     <= 0 by the smallest change in the element's L2 norm,
 //     d <- d - lambda g with lambda = max(0, sum w g.d) / sum w g.g
-//     (an element-wise form of backscatter clipping); clipped elements are
-//     counted.  The correction can then only dissipate kinetic energy.
+//     (an element-wise form of backscatter clipping); projected elements
+//     are counted.  The correction can then only dissipate kinetic energy.
+//     The neutral mode removes the KE production whatever its sign.
+// Training can add Gaussian noise to the normalised features (option
+// input_noise), which makes the network less sensitive to the difference
+// between projected fine states and the coarse solver's own states.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -163,18 +169,39 @@ __global__ void k_channel_stats(const float* __restrict__ D, long rows, int ch, 
   }
 }
 
+// SplitMix64 (Steele, Lea & Flood 2014) as a counter-based hash.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// Standard normal deviate for counter i under key (Box-Muller on two
+// hashed uniforms, the first in (0, 1]).
+__device__ __forceinline__ float normal01(unsigned long long key, long i) {
+  const unsigned long long a = mix64(key ^ (2ULL * (unsigned long long)i));
+  const unsigned long long b = mix64(key ^ (2ULL * (unsigned long long)i + 1ULL));
+  const float u1 = ((float)(a >> 40) + 1.f) * (1.f / 16777216.f);
+  const float u2 = (float)(b >> 40) * (1.f / 16777216.f);
+  return sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+}
+
 // Gathers rows idx[] of raw features/targets and normalises them:
-// Xb = bf16((x - mu_in) / sd_in), Tn = (t - mu_out) / sd_out.
+// Xb = bf16((x - mu_in) / sd_in + noise N(0, sigma^2)), Tn = (t - mu_out) / sd_out.
 __global__ void k_gather_norm(const float* __restrict__ X, const float* __restrict__ Y, const long* __restrict__ idx,
                               int B, int n, const float* __restrict__ mi, const float* __restrict__ si,
                               const float* __restrict__ mo, const float* __restrict__ so,
-                              __nv_bfloat16* __restrict__ Xb, float* __restrict__ Tn) {
+                              __nv_bfloat16* __restrict__ Xb, float* __restrict__ Tn, float noise,
+                              unsigned long long key) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long in_dim = (long)kChIn * n, out_dim = (long)kChOut * n;
   if (i < B * in_dim) {
     const long b = i / in_dim, j = i % in_dim;
     const int c = (int)(j / n);
-    Xb[i] = __float2bfloat16((X[idx[b] * in_dim + j] - mi[c]) / si[c]);
+    float x = (X[idx[b] * in_dim + j] - mi[c]) / si[c];
+    if (noise > 0.f) x += noise * normal01(key, i);
+    Xb[i] = __float2bfloat16(x);
   }
   if (Y && i < B * out_dim) {
     const long b = i / out_dim, j = i % out_dim;
@@ -183,15 +210,11 @@ __global__ void k_gather_norm(const float* __restrict__ X, const float* __restri
   }
 }
 
-// Normalised features beyond this many training standard deviations mark an
-// element as outside the training range.
-constexpr float kOodSigma = 10.f;
-
 // Features of every element of a solver state for inference; ood[e] is set
 // when a feature of element e is outside the training range (or not finite).
 __global__ void k_features(const double* __restrict__ U, const double* __restrict__ Q, int nE, int n,
                            const float* __restrict__ mi, const float* __restrict__ si,
-                           __nv_bfloat16* __restrict__ Xb, int* __restrict__ ood) {
+                           __nv_bfloat16* __restrict__ Xb, int* __restrict__ ood, float ood_sigma) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long in_dim = (long)kChIn * n;
   if (i >= (long)nE * in_dim) return;
@@ -199,7 +222,7 @@ __global__ void k_features(const double* __restrict__ U, const double* __restric
   const int c = (int)(j / n);
   const double v = j < 5 * n ? U[e * 5 * n + j] : Q[e * 15 * n + (j - 5 * n)];
   const float x = ((float)v - mi[c]) / si[c];
-  if (!(fabsf(x) <= kOodSigma)) ood[e] = 1;
+  if (!(fabsf(x) <= ood_sigma)) ood[e] = 1;
   Xb[i] = __float2bfloat16(x);
 }
 
@@ -212,7 +235,7 @@ struct GaussW {
 // non-finite prediction get no correction.
 __global__ void k_correction(const float* __restrict__ Yn, const double* __restrict__ U, int nE, int N,
                              const float* __restrict__ mo, const float* __restrict__ so, const GaussW gw,
-                             const int* __restrict__ ood, double* __restrict__ Kadd,
+                             const int* __restrict__ ood, int energy, double scale, double* __restrict__ Kadd,
                              unsigned long long* __restrict__ counters) {
   const int e = blockIdx.x;
   if (e >= nE) return;
@@ -238,7 +261,7 @@ __global__ void k_correction(const float* __restrict__ Yn, const double* __restr
     const double g0 = -0.5 * (v0 * v0 + v1 * v1 + v2 * v2);
     const double w = gw.w[q % N] * gw.w[(q / N) % N] * gw.w[q / (N * N)];
     double d[4];
-    for (int c = 0; c < 4; ++c) d[c] = (double)(Yn[(long)e * out_dim + c * n + q] * so[c] + mo[c]);
+    for (int c = 0; c < 4; ++c) d[c] = scale * (double)(Yn[(long)e * out_dim + c * n + q] * so[c] + mo[c]);
     pr += w * (g0 * d[0] + v0 * d[1] + v1 * d[2] + v2 * d[3]);
     gg += w * (g0 * g0 + v0 * v0 + v1 * v1 + v2 * v2);
   }
@@ -252,11 +275,14 @@ __global__ void k_correction(const float* __restrict__ Yn, const double* __restr
     }
     __syncthreads();
   }
-  const double lambda = (sp[0] > 0.0 && sg[0] > 0.0) ? sp[0] / sg[0] : 0.0;
+  // energy 1: remove a KE-raising component; energy 2: remove the KE
+  // production whatever its sign; energy 0: no projection
+  const bool project = sg[0] > 0.0 && ((energy == 1 && sp[0] > 0.0) || (energy == 2 && sp[0] != 0.0));
+  const double lambda = project ? sp[0] / sg[0] : 0.0;
   for (int j = threadIdx.x; j < out_dim; j += blockDim.x) {
     const int c = j / n, q = j % n;
-    double d = (double)(Yn[(long)e * out_dim + j] * so[c] + mo[c]);
-    if (lambda > 0.0 && c < 4) {
+    double d = scale * (double)(Yn[(long)e * out_dim + j] * so[c] + mo[c]);
+    if (project && c < 4) {
       const double* u = U + (long)e * 5 * n + q;
       const double ir = 1.0 / u[0];
       const double v0 = u[n] * ir, v1 = u[2 * n] * ir, v2 = u[3 * n] * ir;
@@ -265,7 +291,7 @@ __global__ void k_correction(const float* __restrict__ Yn, const double* __restr
     }
     Kadd[(long)e * out_dim + j] = d;
   }
-  if (lambda > 0.0 && threadIdx.x == 0) atomicAdd(&counters[1], 1ULL);
+  if (project && threadIdx.x == 0) atomicAdd(&counters[1], 1ULL);
 }
 
 __global__ void k_f2bf(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, long count) {
@@ -326,6 +352,7 @@ struct ldg_closure {
   unsigned long long* fallbacks = nullptr;  // [0] elements left uncorrected, [1] elements clipped
   int* ood = nullptr;                       // per element: features outside the training range
   double gw[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // Gauss weights of order p
+  ldg_closure_options opt = {0.f, LDG_CLOSURE_ENERGY_DISSIPATIVE, 1.f, 10.f, 1.f, {0, 0, 0}};
 };
 
 namespace {
@@ -480,13 +507,14 @@ int closure_correction(ldg_closure* c, const SolverView& v, const double* U, con
     cudaError_t e = cudaMemsetAsync(c->ood, 0, sizeof(int) * v.nE, st);
     if (e == cudaSuccess) {
       k_features<<<(unsigned)ceil_div((long)v.nE * c->in_dim, 256), 256, 0, st>>>(U, Q, v.nE, c->n, s, s + 20,
-                                                                                   c->Xb, c->ood);
+                                                                                   c->Xb, c->ood, c->opt.ood_sigma);
       e = forward(c, v.nE);
     }
     if (e == cudaSuccess) {
       GaussW gw;
       for (int i = 0; i < 8; ++i) gw.w[i] = c->gw[i];
-      k_correction<<<v.nE, 128, 0, st>>>(c->Yo, U, v.nE, c->N, s + 40, s + 45, gw, c->ood, Kadd, c->fallbacks);
+      k_correction<<<v.nE, 128, 0, st>>>(c->Yo, U, v.nE, c->N, s + 40, s + 45, gw, c->ood, c->opt.energy,
+                                         (double)c->opt.scale, Kadd, c->fallbacks);
       e = cudaGetLastError();
     }
     if (e != cudaSuccess) rc = fail(LDG_ERR_CUDA, std::string("closure inference: ") + cudaGetErrorString(e));
@@ -683,7 +711,8 @@ int ldg_closure_train(ldg_closure* c, long long first, long long count, int iter
     for (int b = 0; b < batch; ++b) idx[b] = (long)pick(rng);
     CL_CUDA(cudaMemcpyAsync(c->idx, idx.data(), sizeof(long) * batch, cudaMemcpyHostToDevice, c->stream));
     k_gather_norm<<<(unsigned)ceil_div((long)batch * c->in_dim, 256), 256, 0, c->stream>>>(
-        c->X, c->Y, c->idx, batch, c->n, s, s + 20, s + 40, s + 45, c->Xb, c->Tn);
+        c->X, c->Y, c->idx, batch, c->n, s, s + 20, s + 40, s + 45, c->Xb, c->Tn, c->opt.input_noise,
+        seed * 0x100000001B3ULL + (unsigned long long)it);
     CL_CUDA(forward(c, batch));
     k_mse_grad<<<(unsigned)ceil_div(batch, 128), 128, 0, c->stream>>>(c->Yo, c->Tn, c->dY, c->dYb, batch,
                                                                       c->out_dim, c->rowl);
@@ -691,8 +720,11 @@ int ldg_closure_train(ldg_closure* c, long long first, long long count, int iter
     CL_CUDA(backward(c, batch));
     c->adam_t += 1;
     const float c1 = 1.f - std::pow(b1, (float)c->adam_t), c2 = 1.f - std::pow(b2, (float)c->adam_t);
+    // cosine decay from lr to lr * lr_final over the call (constant when lr_final = 1)
+    const float frac = iters > 1 ? (float)it / (float)(iters - 1) : 0.f;
+    const float lr_it = lr * (c->opt.lr_final + (1.f - c->opt.lr_final) * 0.5f * (1.f + std::cos(3.14159265f * frac)));
     k_adam<<<(unsigned)ceil_div(c->n_params, 256), 256, 0, c->stream>>>(
-        c->theta, c->grad, c->m, c->v, c->wb, nullptr, 1, 1, c->n_params, lr, b1, b2, eps, c1, c2);
+        c->theta, c->grad, c->m, c->v, c->wb, nullptr, 1, 1, c->n_params, lr_it, b1, b2, eps, c1, c2);
     CL_CUDA(cudaGetLastError());
     // the bf16 copies of the biases are unused; the weights' are refreshed
     // by k_adam (same offsets)
@@ -721,7 +753,7 @@ int ldg_closure_evaluate(ldg_closure* c, long long first, long long count, doubl
     for (int i = 0; i < nb; ++i) idx[i] = (long)(b0 + i);
     CL_CUDA(cudaMemcpyAsync(c->idx, idx.data(), sizeof(long) * nb, cudaMemcpyHostToDevice, c->stream));
     k_gather_norm<<<(unsigned)ceil_div((long)nb * c->in_dim, 256), 256, 0, c->stream>>>(
-        c->X, c->Y, c->idx, nb, c->n, s, s + 20, s + 40, s + 45, c->Xb, c->Tn);
+        c->X, c->Y, c->idx, nb, c->n, s, s + 20, s + 40, s + 45, c->Xb, c->Tn, 0.f, 0ULL);
     CL_CUDA(forward(c, nb));
     k_eval_rows<<<(unsigned)ceil_div(nb, 128), 128, 0, c->stream>>>(c->Yo, c->Tn, nb, c->n, s + 40, s + 45,
                                                                     c->evalbuf);
@@ -754,6 +786,10 @@ int ldg_closure_get_params(ldg_closure* c, float* out) {
 int ldg_closure_set_params(ldg_closure* c, const float* in) {
   if (!c || !in) return fail(LDG_ERR_INVALID, "closure: null argument");
   CL_CUDA(cudaMemcpyAsync(c->theta, in, sizeof(float) * c->n_params, cudaMemcpyHostToDevice, c->stream));
+  // new parameters restart the optimiser
+  CL_CUDA(cudaMemsetAsync(c->m, 0, sizeof(float) * c->n_params, c->stream));
+  CL_CUDA(cudaMemsetAsync(c->v, 0, sizeof(float) * c->n_params, c->stream));
+  c->adam_t = 0;
   int rc = refresh_bf16(c);
   if (rc) return rc;
   CL_CUDA(cudaStreamSynchronize(c->stream));
@@ -819,6 +855,21 @@ int ldg_closure_get_samples(ldg_closure* c, long long first, long long count, fl
 
 int ldg_closure_fallbacks(ldg_closure* c, long long* count) {
   return ldg_closure_counters(c, count, nullptr);
+}
+
+int ldg_closure_get_options(const ldg_closure* c, ldg_closure_options* o) {
+  if (!c || !o) return fail(LDG_ERR_INVALID, "closure: null argument");
+  *o = c->opt;
+  return LDG_OK;
+}
+
+int ldg_closure_set_options(ldg_closure* c, const ldg_closure_options* o) {
+  if (!c || !o) return fail(LDG_ERR_INVALID, "closure: null argument");
+  if (!(o->input_noise >= 0.f) || o->energy < 0 || o->energy > 2 || !(o->scale >= 0.f) || !(o->ood_sigma > 0.f) ||
+      !(o->lr_final > 0.f && o->lr_final <= 1.f))
+    return fail(LDG_ERR_INVALID, "closure: bad options");
+  c->opt = *o;
+  return LDG_OK;
 }
 
 int ldg_closure_counters(ldg_closure* c, long long* fallbacks, long long* clipped) {

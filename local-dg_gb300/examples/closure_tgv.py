@@ -26,10 +26,17 @@ fine FP64 evaluation run:
                 raises an element's kinetic energy) and falls back to plain
                 LDG outside the training range
 
+One data set can train several closure variants (--variants, a JSON list):
+each entry sets the training options (input_noise, lr_final) and lists the
+inference modes ([energy, scale] or [energy, scale, ood_sigma]) to run a
+posteriori; the network is re-initialised between variants.
+--coarse-nx/--fine-nx shrink the meshes for quick studies (defaults: the
+16^3 / 32^3 experiment).
+
 Writes a JSON summary after each phase (a partial run still reports) and
 the raw KE series to <out>.npz.  Usage:
     python local-dg_gb300/examples/closure_tgv.py --out results.json \
-        [--t-end 20] [--sample-dt 0.5] [--iters 10000]
+        [--t-end 20] [--sample-dt 0.5] [--iters 10000] [--variants '[...]']
 """
 from __future__ import annotations
 
@@ -48,8 +55,11 @@ import ldg  # noqa: E402
 
 SEED_TRAIN = 1001
 SEED_EVAL = 2002
-COARSE = (16, 2)
-FINE = (32, 4)
+P_COARSE, P_FINE = 2, 4
+DEFAULT_VARIANTS = [
+    {"name": "noise-0.3", "input_noise": 0.3, "lr_final": 0.05,
+     "modes": [["dissipative", 1.0, 10.0], ["dissipative", 1.0, 30.0]]},
+]
 
 
 def dt_for(nx, p, cfl):
@@ -91,9 +101,13 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--hidden", type=int, default=128)
     ap.add_argument("--amp", type=float, default=1e-2)
+    ap.add_argument("--coarse-nx", type=int, default=16)
+    ap.add_argument("--fine-nx", type=int, default=32)
+    ap.add_argument("--variants", default=None, help="JSON list of closure variants")
     args = ap.parse_args()
-    res = {"config": vars(args), "coarse": "16^3 p=2 FP64, CFL 0.01",
-           "fine": f"32^3 p=4 FP64, CFL {args.fine_cfl}",
+    variants = json.loads(args.variants) if args.variants else DEFAULT_VARIANTS
+    res = {"config": vars(args), "coarse": f"{args.coarse_nx}^3 p=2 FP64, CFL 0.01",
+           "fine": f"{args.fine_nx}^3 p=4 FP64, CFL {args.fine_cfl}", "variants": variants,
            "seeds": {"train": [[SEED_TRAIN, 0], [SEED_TRAIN, 1]], "eval": [SEED_EVAL, 0]}}
     series = {}
 
@@ -102,8 +116,9 @@ def main():
             json.dump(res, f, indent=1)
         np.savez(os.path.splitext(args.out)[0] + ".npz", **series)
 
-    (ncx, pc), (nfx, pf) = COARSE, FINE
+    (ncx, pc), (nfx, pf) = (args.coarse_nx, P_COARSE), (args.fine_nx, P_FINE)
     closure = ldg.Closure(p=pc, hidden=args.hidden, seed=7)
+    theta0 = closure.get_params()
     coarse_ws = ldg.Solver(pc, ncx, steps=10)
 
     dt_f = dt_for(nfx, pf, args.fine_cfl)
@@ -143,32 +158,14 @@ def main():
     res["eval_run"] = {"steps": fine_steps, "dt": dt_eval, "seconds": time.perf_counter() - t0}
     save()
 
-    # ---- training on the GPU
-    t0 = time.perf_counter()
+    # ---- a posteriori reference: the plain coarse LDG run
     closure.finalize(0, n_train)
-    losses = closure.train(0, n_train, iters=args.iters, batch=args.batch, lr=args.lr, seed=3)
-    series["losses"] = losses
-    e_plain, e_closure = closure.evaluate(n_train, n_held)
-    e_plain_tr, e_closure_tr = closure.evaluate(0, n_train)
-    per = n_held // n_times
-    by_time = []
-    for k in range(n_times):
-        a, b = closure.evaluate(n_train + k * per, per)
-        by_time.append([k * per_sample * dt_eval, a, b])
-    res["training"] = {"seconds": time.perf_counter() - t0, "samples": n_train, "params": closure.n_params,
-                       "loss_first50": float(np.mean(losses[:50])), "loss_last50": float(np.mean(losses[-50:]))}
-    res["a_priori"] = {"heldout_samples": n_held, "rhs_err_plain": e_plain, "rhs_err_closure": e_closure,
-                       "train_rhs_err_plain": e_plain_tr, "train_rhs_err_closure": e_closure_tr,
-                       "heldout_by_time": by_time,
-                       "units": "mean squared RHS error over the normalised target channels"}
-    save()
-
-    # ---- a posteriori: coarse plain / closure against the fine evaluation run
     nc_steps = int(math.ceil(args.t_end / dt_for(ncx, pc, 0.01)))
-    for name, use in (("plain", False), ("closure", True)):
+
+    def coarse_run(name, attach):
         t0 = time.perf_counter()
         with ldg.Solver(pc, ncx, steps=nc_steps, perturb_amp=args.amp, seed=SEED_EVAL, instance=0) as s:
-            if use:
+            if attach:
                 s.attach_closure(closure)
             status, done = "ok", 0
             try:
@@ -181,23 +178,54 @@ def main():
             ke = s.ke_history()
             bad = np.flatnonzero(~np.isfinite(ke))
             series["ke_" + name] = ke[:bad[0]] if bad.size else ke
-            res.setdefault("coarse_runs", {})[name] = {"status": status, "dt": s.dt,
-                                                       "seconds": time.perf_counter() - t0}
+            return {"status": status, "dt": s.dt, "seconds": time.perf_counter() - t0}
+
     tf_, ef = dissipation(series["ke_fine"], dt_eval)
     scale = float(np.max(ef))
-    summary = {"fine": compare("fine", series["ke_fine"], dt_eval, tf_, ef, scale)}
-    for name in ("plain", "closure"):
-        summary[name] = compare(name, series["ke_" + name], res["coarse_runs"][name]["dt"], tf_, ef, scale)
-        summary[name]["status"] = res["coarse_runs"][name]["status"]
-    summary["closure_fallback_element_stages"] = closure.fallbacks
-    summary["closure_clipped_element_stages"] = closure.clipped
+    info = coarse_run("plain", False)
+    summary = {"fine": compare("fine", series["ke_fine"], dt_eval, tf_, ef, scale),
+               "plain": dict(compare("plain", series["ke_plain"], info["dt"], tf_, ef, scale), **info)}
     res["a_posteriori"] = summary
     save()
+
+    # ---- each variant: train on the GPU, a priori error, a posteriori runs
+    res["training"], res["a_priori"] = {}, {}
+    per = n_held // n_times
+    for var in variants:
+        vn = var["name"]
+        t0 = time.perf_counter()
+        closure.set_params(theta0)
+        closure.set_options(input_noise=float(var.get("input_noise", 0.0)),
+                            lr_final=float(var.get("lr_final", 1.0)))
+        losses = closure.train(0, n_train, iters=args.iters, batch=args.batch, lr=args.lr, seed=3)
+        series["losses_" + vn] = losses
+        e_plain, e_closure = closure.evaluate(n_train, n_held)
+        e_plain_tr, e_closure_tr = closure.evaluate(0, n_train)
+        by_time = []
+        for k in range(n_times):
+            a, b = closure.evaluate(n_train + k * per, per)
+            by_time.append([k * per_sample * dt_eval, a, b])
+        res["training"][vn] = {"seconds": time.perf_counter() - t0, "samples": n_train,
+                               "params": closure.n_params, "loss_first50": float(np.mean(losses[:50])),
+                               "loss_last50": float(np.mean(losses[-50:]))}
+        res["a_priori"][vn] = {"heldout_samples": n_held, "rhs_err_plain": e_plain, "rhs_err_closure": e_closure,
+                               "train_rhs_err_plain": e_plain_tr, "train_rhs_err_closure": e_closure_tr,
+                               "heldout_by_time": by_time,
+                               "units": "mean squared RHS error over the normalised target channels"}
+        for mode in var["modes"]:
+            energy, fac = mode[0], float(mode[1])
+            ood = float(mode[2]) if len(mode) > 2 else 10.0
+            name = f"{vn}/{energy}/x{fac:g}/ood{ood:g}"
+            closure.set_options(energy=energy, scale=fac, ood_sigma=ood)
+            f0, c0 = closure.fallbacks, closure.clipped
+            info = coarse_run(name, True)
+            summary[name] = dict(compare(name, series["ke_" + name], info["dt"], tf_, ef, scale), **info)
+            summary[name]["fallback_element_stages"] = closure.fallbacks - f0
+            summary[name]["projected_element_stages"] = closure.clipped - c0
+            save()
     closure.close()
     coarse_ws.close()
-    print(json.dumps({k: res[k] for k in ("train_runs", "eval_run", "training", "a_priori", "a_posteriori")},
-                     indent=1))
-
+    print(json.dumps({k: res[k] for k in ("train_runs", "eval_run", "training", "a_posteriori")}, indent=1))
 
 if __name__ == "__main__":
     main()

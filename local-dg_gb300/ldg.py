@@ -109,6 +109,13 @@ class LdgInfo(ctypes.Structure):
     ]
 
 
+class LdgClosureOptions(ctypes.Structure):
+    _fields_ = [("input_noise", ctypes.c_float), ("energy", ctypes.c_int), ("scale", ctypes.c_float),
+                ("ood_sigma", ctypes.c_float), ("lr_final", ctypes.c_float), ("reserved", ctypes.c_int * 3)]
+
+
+CLOSURE_ENERGY = {"none": 0, "dissipative": 1, "neutral": 2}
+
 # Every symbol include/ldg.h declares, with its ctypes signature.
 _vp, _i, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -163,6 +170,8 @@ SIGNATURES = {
                                       ctypes.POINTER(ctypes.c_float)]),
     "ldg_closure_fallbacks": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
     "ldg_closure_counters": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+    "ldg_closure_get_options": (_i, [_vp, ctypes.POINTER(LdgClosureOptions)]),
+    "ldg_closure_set_options": (_i, [_vp, ctypes.POINTER(LdgClosureOptions)]),
     "ldg_closure_get_samples": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(ctypes.c_float),
                                      ctypes.POINTER(ctypes.c_float)]),
     "ldg_solver_attach_closure": (_i, [_vp, _vp]),
@@ -539,6 +548,25 @@ class Closure:
         Y = np.zeros((count, self.out_dim), dtype=np.float32)
         _check(load().ldg_closure_get_samples(self._h, first, count, _fp(X), _fp(Y)), "ldg_closure_get_samples")
         return X, Y
+
+    def options(self) -> dict:
+        o = LdgClosureOptions()
+        _check(load().ldg_closure_get_options(self._h, ctypes.byref(o)), "ldg_closure_get_options")
+        energy = {v: k for k, v in CLOSURE_ENERGY.items()}[o.energy]
+        return {"input_noise": o.input_noise, "energy": energy, "scale": o.scale, "ood_sigma": o.ood_sigma,
+                "lr_final": o.lr_final}
+
+    def set_options(self, **kw) -> None:
+        """input_noise, energy ('none' | 'dissipative' | 'neutral'), scale,
+        ood_sigma, lr_final (ldg_closure_set_options)."""
+        cur = self.options()
+        unknown = set(kw) - set(cur)
+        if unknown:
+            raise TypeError(f"unknown closure options {sorted(unknown)}")
+        cur.update(kw)
+        o = LdgClosureOptions(cur["input_noise"], CLOSURE_ENERGY[cur["energy"]], cur["scale"], cur["ood_sigma"],
+                              cur["lr_final"])
+        _check(load().ldg_closure_set_options(self._h, ctypes.byref(o)), "ldg_closure_set_options")
 
     @property
     def clipped(self) -> int:

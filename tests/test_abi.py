@@ -34,13 +34,15 @@ def test_struct_layouts_match_header(tmp_path):
         pytest.skip("no C compiler")
     src = tmp_path / "sz.c"
     src.write_text('#include "ldg.h"\n#include <stdio.h>\n#include <stddef.h>\n'
-                   'int main(){printf("%zu %zu %zu %zu\\n", sizeof(ldg_config), sizeof(ldg_info),'
-                   ' offsetof(ldg_config, box_lo), offsetof(ldg_info, device_bytes));}\n')
+                   'int main(){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(ldg_config), sizeof(ldg_info),'
+                   ' offsetof(ldg_config, box_lo), offsetof(ldg_info, device_bytes),'
+                   ' sizeof(ldg_closure_options), offsetof(ldg_closure_options, lr_final));}\n')
     exe = tmp_path / "sz"
     subprocess.run([cc, "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     assert got == [ctypes.sizeof(ldg.LdgConfig), ctypes.sizeof(ldg.LdgInfo),
-                   ldg.LdgConfig.box_lo.offset, ldg.LdgInfo.device_bytes.offset]
+                   ldg.LdgConfig.box_lo.offset, ldg.LdgInfo.device_bytes.offset,
+                   ctypes.sizeof(ldg.LdgClosureOptions), ldg.LdgClosureOptions.lr_final.offset]
 
 
 def test_config_defaults_follow_reference():

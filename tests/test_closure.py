@@ -145,6 +145,12 @@ def test_attached_correction_never_raises_element_kinetic_energy():
             a.attach_closure(c)
             k_cl = a.rhs(u)
             clipped = c.clipped
+            c.set_options(energy="neutral")
+            k_neutral = a.rhs(u)
+            assert c.options()["energy"] == "neutral"
+            with pytest.raises(ldg.LdgError):
+                c.set_options(scale=-1.0)
+            c.set_options(energy="dissipative")
     o = oracle.Oracle(4, 2)
     n = 27
     I3 = o.operator(1).reshape(n, n, order="F")
@@ -158,3 +164,8 @@ def test_attached_correction_never_raises_element_kinetic_energy():
     scale = np.sum(w3 * (np.abs(g0 * D[:, 0]) + np.sum(np.abs(v * D[:, 1:4]), axis=1)), axis=1)
     assert np.all(prod <= 1e-10 * scale + 1e-300), prod.max()
     assert clipped >= 0
+    # the neutral mode removes the KE production entirely
+    Dn = np.einsum("qi,evi->evq", I3, k_neutral - k_plain)
+    prod_n = np.sum(w3 * (g0 * Dn[:, 0] + np.sum(v * Dn[:, 1:4], axis=1)), axis=1)
+    scale_n = np.sum(w3 * (np.abs(g0 * Dn[:, 0]) + np.sum(np.abs(v * Dn[:, 1:4]), axis=1)), axis=1)
+    assert np.all(np.abs(prod_n) <= 1e-10 * scale_n + 1e-300)

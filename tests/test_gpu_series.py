@@ -33,7 +33,8 @@ def load(name):
 @pytest.mark.parametrize("name", ["series_n32_p3.npz", "series_n64_p4.npz"])
 def test_benchmark_mesh_per_step_parity(name):
     z = load(name)
-    nx, p = int(name.split("_")[1][1:]), int(name.split("_")[2][1:3])
+    stem = name.split(".")[0]  # series_n<nx>_p<p>
+    nx, p = int(stem.split("_")[1][1:]), int(stem.split("_")[2][1:])
     steps = int(z["steps"])
     idx = z["idx"]
     worst = 0.0
@@ -87,7 +88,8 @@ def enstrophy_numpy(u_nodal, q_nodal, nx, p, L=1.0):
 @pytest.mark.parametrize("name", ["rhs_n3_p2.npz", "rhs_n4_p3.npz", "rhs_n3_p4.npz"])
 def test_enstrophy_matches_reference_gradient(name):
     z = load(name)
-    nx, p = int(name.split("_")[1][1:]), int(name.split("_")[2][1])
+    stem = name.split(".")[0]  # rhs_n<nx>_p<p>
+    nx, p = int(stem.split("_")[1][1:]), int(stem.split("_")[2][1:])
     ref = enstrophy_numpy(z["u0"], z["q"], nx, p)
     with ldg.Solver(p, nx) as s:
         s.set_state(z["u0"])
