@@ -43,30 +43,17 @@ BYTES_GRAD = 8 * (5 + 15)        # read U, write q
 BYTES_RHS = 8 * (5 + 15 + 5)     # read U, read q, write k / next stage
 
 
-def fp64_flops_per_element_stage(N: int) -> float:
-    """FP64 floating-point operations the sum-factorised kernels perform per
-    element and RK stage (counted from the kernels; FMA = 2).  Divisions and
-    square roots are counted as one operation each here."""
-    n, nf = N ** 3, N ** 2
-    grad = (3 * 5 * 2 * N * n          # A_l contractions of U
-            + 3 * 5 * 4 * n            # lifts (2 FMA) + scale
-            + 3 * 15 * 2 * N * nf)     # minus-face traces of q
-    vol = n * (13 + 5 * 3 + 9 * 3 + 3 * 9 + 20 + 3 * 12 + 15)  # Euler + viscous flux per point
-    face = 6 * nf * (110 + 60)         # Roe + one viscous column per face point
-    rhs = (vol + face
-           + 3 * 5 * 2 * N * n         # A_l contractions of F
-           + 6 * 5 * 2 * n             # face lifts
-           + 5 * 4 * n                 # RK update
-           + 6 * 5 * 2 * N * nf)       # traces of the next stage
-    return float(grad + rhs)
-
-
-# DRAM bytes (read + write) per element per launch from one ncu capture of
-# the same kernels at 24^3 p=4 (profiles/ncu_k_grad_k_rhs_fp64_tgv24_p4.md),
-# scaled to a launch by the element count (traffic grows with elements).
-NCU_TRAFFIC_PER_ELEMENT = {
-    ("rhs", 5, "fp64"): (608.591872e6 + 192.881408e6) / 13824,
-    ("grad", 5, "fp64"): (116.264960e6 + 271.343104e6) / 13824,
+# Per element and launch, from one ncu --set full capture of the same
+# kernels at 24^3 p=4 (13,824 elements; DRAM traffic and instruction counts
+# grow in proportion to the element count): DRAM bytes read + written, and
+# FP64 floating-point operations executed (2 per DFMA, 1 per DMUL or DADD;
+# k_grad: 21,825 DFMA + 5,400 DMUL + 3,075 DADD; k_rhs: 28,800 + 6,000 +
+# 3,300).
+NCU_PER_ELEMENT = {
+    ("grad", 5, "fp64"): {"dram_bytes": (152.857088e6 + 313.136896e6) / 13824, "fp64_flops": 52125.0},
+    ("rhs", 5, "fp64"): {"dram_bytes": (649.381632e6 + 189.743360e6) / 13824, "fp64_flops": 66900.0},
+    ("grad", 5, "mixed"): {"dram_bytes": (152.870400e6 + 312.989952e6) / 13824},
+    ("rhs", 5, "mixed"): {"dram_bytes": (649.710080e6 + 189.202176e6) / 13824},
 }
 
 
@@ -356,21 +343,22 @@ def run_ours(args):
     alg_bytes = per_dof * s.dofs * s.nE
     achieved = alg_bytes / avg_s / 1e9
     N = args.p + 1
-    fp64_peak = ldg.probe_fp64_peak(dev)
-    flops_step = fp64_flops_per_element_stage(N) * s.nE * 4
-    fp64_achieved = flops_step * K / (ms * 1e-3) / 1e12
-    tpe = NCU_TRAFFIC_PER_ELEMENT.get((dom, N, args.precision))
+    ncu = NCU_PER_ELEMENT.get((dom, N, args.precision), {})
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": tpe * s.nE if tpe else None,
+                "frac": achieved / hbm_peak,
+                "traffic": ncu["dram_bytes"] * s.nE if "dram_bytes" in ncu else None,
                 "algorithmic_bytes": alg_bytes,
-                "kernel": f"k_rhs<{N},{'double' if args.precision == 'fp64' else 'dd'}>" if dom == "rhs"
-                else f"k_grad<{N}>",
+                "kernel": f"k_{dom}<{N},{'double' if args.precision == 'fp64' else 'dd'}>",
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
-    if args.precision == "fp64":
-        roofline["binding_roof"] = {"pipe": "fp64", "achieved_tflops": fp64_achieved,
-                                    "peak_tflops": fp64_peak, "frac": fp64_achieved / fp64_peak,
+    if "fp64_flops" in ncu:
+        # the pipe that binds: FP64 operations per launch of the same kernel
+        fp64_peak = ldg.probe_fp64_peak(dev)
+        fp64_achieved = ncu["fp64_flops"] * s.nE / avg_s / 1e12
+        roofline["binding_roof"] = {"pipe": "fp64", "achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak,
+                                    "frac": fp64_achieved / fp64_peak,
                                     "peak_source": "measured (ldg_probe_fp64_peak FMA chain)",
-                                    "flops_per_dof_stage": fp64_flops_per_element_stage(N) / N ** 3}
+                                    "flops_per_dof": ncu["fp64_flops"] / N ** 3,
+                                    "flops_source": "ncu instruction counts, 24^3 p=4 capture"}
     kernel_ms = {k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1)} for k, v in kt.items()}
     s.close()
 

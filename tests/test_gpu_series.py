@@ -49,8 +49,13 @@ def test_benchmark_mesh_per_step_parity(name):
             err = rel_l2(u.ravel()[idx], z["samples"][k])
             worst = max(worst, err)
             assert err <= TOL, (k + 1, err)
-            norms = np.einsum("evq,evq->v", u, u)
-            assert np.max(np.abs(norms - z["norms"][k]) / z["norms"][k]) <= TOL, k + 1
+            # each variable's L2 norm, against the whole state's norm (the
+            # per-step relative-L2 bar; a variable such as the w momentum
+            # can be 1e-15 of the state, so its own relative error is not
+            # the measure)
+            norms = np.sqrt(np.einsum("evq,evq->v", u, u))
+            ref = np.sqrt(z["norms"][k])
+            assert np.max(np.abs(norms - ref)) <= TOL * np.sqrt(np.sum(z["norms"][k])), k + 1
             if nx == 32 and (k + 1) % 20 == 0:
                 enst.append(s.diagnostics()[2])
         ke = s.ke_history()
