@@ -110,6 +110,10 @@ __device__ __forceinline__ bool not_finite(double x) {
 // helpers that are exact in both types
 __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
 __device__ __forceinline__ double half_(double x) { return 0.5 * x; }
+// 1/sqrt(x): CUDA's double rsqrt; on the FP32-pair path the pair reciprocal
+// of the pair square root.
+__device__ __forceinline__ double rsqrt_(double x) { return ::rsqrt(x); }
+__device__ __forceinline__ dd rsqrt_(dd x) { return rcp(sqrt(x)); }
 __device__ __forceinline__ dd half_(dd x) { return scale2(x, 0.5f); }
 template <class T>
 __device__ __forceinline__ T sgn(bool plus, T x) { return plus ? x : -x; }
@@ -210,13 +214,18 @@ template <int l, class T>
 __device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool s, const OpsT<T>& o,
                                          T F[kNS]) {
   T rN = uN[0], rK = uK[0];
-  T irN = rcp(rN), irK = rcp(rK);
+  // One reciprocal square root s2 = 1/sqrt(rho_N rho_K) gives both inverse
+  // densities (rho_K s2^2, rho_N s2^2) and the Roe weight sqrt(rho_N/rho_K)
+  // = rho_N s2.
+  T s2 = rsqrt_(rN * rK);
+  T ip = s2 * s2;
+  T irN = rK * ip, irK = rN * ip;
   T vN[3] = {uN[1] * irN, uN[2] * irN, uN[3] * irN};
   T vK[3] = {uK[1] * irK, uK[2] * irK, uK[3] * irK};
   T qN = sgn(s, vN[l]), qK = sgn(s, vK[l]);
   T pN = o.g1 * uN[4] - o.hg1 * rN * (vN[0] * vN[0] + vN[1] * vN[1] + vN[2] * vN[2]);
   T pK = o.g1 * uK[4] - o.hg1 * rK * (vK[0] * vK[0] + vK[1] * vK[1] + vK[2] * vK[2]);
-  T sq = sqrt(rN * irK);
+  T sq = rN * s2;
   T is1 = rcp(sq + o.one);
   T vt[3];
 #pragma unroll
@@ -225,9 +234,9 @@ __device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool 
   T vt2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
   T qt = sgn(s, vt[l]);
   T c2 = o.g1 * (Ht - half_(vt2));
-  T ic2 = rcp(c2);
-  T c = sqrt(c2);
-  T ic = c * ic2;  // 1/c
+  T ic = rsqrt_(c2);  // 1/c
+  T c = c2 * ic;
+  T ic2 = ic * ic;
   T l0 = fabs(qt);
   T lp = half_(fabs(qt + c)), lm = half_(fabs(c - qt));
   T dr = rN - rK;
