@@ -47,10 +47,10 @@ BYTES_RHS = 8 * (5 + 15 + 5)     # read U, read q, write k / next stage
 # kernels at 24^3 p=4 (13,824 elements; DRAM traffic and instruction counts
 # grow in proportion to the element count): DRAM bytes read + written, and
 # FP64 floating-point operations executed (2 per DFMA, 1 per DMUL or DADD;
-# k_grad: 21,825 DFMA + 5,400 DMUL + 3,075 DADD; k_rhs: 28,800 + 6,000 +
+# k_grad: 20,550 DFMA + 5,550 DMUL + 2,925 DADD; k_rhs: 28,800 + 6,000 +
 # 3,300).
 NCU_PER_ELEMENT = {
-    ("grad", 5, "fp64"): {"dram_bytes": (152.857088e6 + 313.136896e6) / 13824, "fp64_flops": 52125.0},
+    ("grad", 5, "fp64"): {"dram_bytes": (152.824320e6 + 313.398784e6) / 13824, "fp64_flops": 49575.0},
     ("rhs", 5, "fp64"): {"dram_bytes": (649.381632e6 + 189.743360e6) / 13824, "fp64_flops": 66900.0},
     ("grad", 5, "mixed"): {"dram_bytes": (152.870400e6 + 312.989952e6) / 13824},
     ("rhs", 5, "mixed"): {"dram_bytes": (649.710080e6 + 189.202176e6) / 13824},
