@@ -192,7 +192,7 @@ template <int N>
 size_t smem_traces() { return sizeof(double) * Cfg<N>::EPC * kNS * Cfg<N>::n; }
 template <int N>
 size_t smem_grad() {
-  return sizeof(double) * Cfg<N>::EPC * (kNS * Cfg<N>::n + kNQ * Cfg<N>::n + 9 * kNS * Cfg<N>::nf + Cfg<N>::n);
+  return sizeof(double) * Cfg<N>::EPC * grad_smem_values_per_element<N>();
 }
 template <int N>
 size_t smem_rhs() {

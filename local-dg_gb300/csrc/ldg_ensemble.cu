@@ -192,7 +192,8 @@ size_t smem_bytes(int BD) {
   size_t mx = 0;
   for (int N = 3; N <= 5; ++N) {
     const size_t E = tile_epc(N, BD), n = (size_t)N * N * N, nf = (size_t)N * N;
-    mx = std::max(mx, sizeof(double) * E * (kNS * n + kNQ * n + 9 * kNS * nf + n));
+    // grad_body's layout (grad_smem_values_per_element) and rhs_body's
+    mx = std::max(mx, sizeof(double) * E * (kNS * n + 2 * 3 * kNS * nf + kNQ * n + n));
     mx = std::max(mx, sizeof(double) * E * (kNQ * n + 6 * kNS * nf));
   }
   return mx;

@@ -162,6 +162,15 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_traces(const double* __restrict__
 // side of every face, so only plus-face traces are read.
 // Writes Q and the minus-face traces Tq; on the FP64 path optionally the
 // per-element enstrophy.
+// Shared memory of grad_body, in 8-byte values per element: U (5n), the +l
+// traces of the element and of its -l neighbours (2 x 15 nf), the element's
+// own -l traces (15 nf, needed by the Roe phase only) whose space Q (15 n)
+// reuses after that phase, and the enstrophy density (n).
+template <int N>
+constexpr int grad_smem_values_per_element() {
+  return kNS * N * N * N + 2 * 3 * kNS * N * N + kNQ * N * N * N + N * N * N;
+}
+
 template <int N, class T, int E = DefEPC<N>::value>
 __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict__ U,
                                           const typename Real<T>::S* __restrict__ Tu,
@@ -172,12 +181,13 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
                                           double* smem_raw) {
   constexpr int n = Cfg<N, E>::n, nf = Cfg<N, E>::nf, EPC = Cfg<N, E>::EPC, NT = Cfg<N, E>::T;
   using R = Real<T>;
+  static_assert(kNQ * n >= 3 * kNS * nf, "Q must cover the -l trace space it reuses");
   T* sU = reinterpret_cast<T*>(smem_raw);  // EPC*5*n
-  T* sQ = sU + EPC * kNS * n;              // EPC*15*n
-  T* sTp = sQ + EPC * kNQ * n;             // EPC*3*5*nf  own +l traces
+  T* sTp = sU + EPC * kNS * n;             // EPC*3*5*nf  own +l traces
   T* sTm = sTp + EPC * 3 * kNS * nf;       // EPC*3*5*nf  (-l neighbour)'s +l traces
-  T* sTo = sTm + EPC * 3 * kNS * nf;       // EPC*3*5*nf  own -l traces
-  double* sE = reinterpret_cast<double*>(sTo + EPC * 3 * kNS * nf);  // EPC*n enstrophy
+  T* sTo = sTm + EPC * 3 * kNS * nf;       // EPC*3*5*nf  own -l traces (Roe phase)
+  T* sQ = sTo;                             // EPC*15*n, reuses sTo after the Roe phase
+  double* sE = reinterpret_cast<double*>(sQ + EPC * kNQ * n);  // EPC*n enstrophy
   for (int i = threadIdx.x; i < ne * kNS * n; i += NT) sU[i] = R::ld(U + e0 * kNS * n + i);
   for (int i = threadIdx.x; i < ne * 3 * kNS * nf; i += NT) {
     int es = i / (3 * kNS * nf);
@@ -210,6 +220,7 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
 #pragma unroll
     for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + v * nf + t, F[v]);
   }
+  __syncthreads();  // the own -l traces are dead: Q takes their space
   const int es = threadIdx.x / n, q = threadIdx.x % n;
   if (es < ne) {
     const int c[3] = {q % N, (q / N) % N, q / (N * N)};
@@ -280,7 +291,7 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
 }
 
 template <int N, class T>
-__global__ void __launch_bounds__(Cfg<N>::T) k_grad(const typename Real<T>::S* __restrict__ U,
+__global__ void __launch_bounds__(Cfg<N>::T, Cfg<N>::T == 256 ? 4 : 1) k_grad(const typename Real<T>::S* __restrict__ U,
                                                     const typename Real<T>::S* __restrict__ Tu,
                                                     typename Real<T>::S* __restrict__ Q,
                                                     typename Real<T>::S* __restrict__ Tq,

@@ -77,7 +77,7 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   double* Fm = Tq + ne * 3 * kNQ * C::nf;    // [nE][3][5][nf] minus-face Roe fluxes
   const size_t sm_tr = sizeof(double) * 2 * C::EPC * kNS * C::n;
   const size_t sm_trc = sizeof(double) * C::EPC * kNS * C::n;
-  const size_t sm_g = sizeof(double) * C::EPC * (kNS * C::n + kNQ * C::n + 9 * kNS * C::nf + C::n);
+  const size_t sm_g = sizeof(double) * C::EPC * grad_smem_values_per_element<N>();
   const size_t sm_r = sizeof(double) * C::EPC * (kNQ * C::n + 6 * kNS * C::nf);
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(k_transform<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tr)) ||
