@@ -969,7 +969,6 @@ int ldg_step(ldg_solver* s, int nsteps) {
       c.Tu = Tu_in;
       c.Tq = s->Tq;
       c.Fm = s->Fm;
-  c.Fm = s->Fm;
       c.Un = s->Un;
       c.Uacc = s->Uacc;
       c.Unext = (stage < 3 || mixed) ? (void*)s->Us : nullptr;
