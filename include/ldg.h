@@ -209,6 +209,11 @@ int ldg_kernel_times(ldg_solver* s, double* ms, long long* launches, int max_cla
  * a register-resident FMA chain; the roofline denominator for the FP64
  * kernels.  (No reference counterpart.) */
 int ldg_probe_fp64_peak(int device, double* tflops);
+/* The same probe with two more readings: FP64 FMAs issued per SM per SM
+ * clock (from clock64 spans, independent of the clock frequency) and the
+ * SM clock the probe ran at, in MHz (cycles over event time).  Either
+ * pointer may be NULL.  (No reference counterpart.) */
+int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* sm_mhz);
 
 /* ---- Batched ensemble.  No reference counterpart (the reference runs one
  * problem per MPI job).  Members are independent problems, each an
@@ -321,7 +326,9 @@ int ldg_solver_attach_closure(ldg_solver* s, ldg_closure* c);
  * fragmentation) is not allowed.  Such callers cannot use ldg_create, which
  * allocates the solver's buffers.
  *
- * Computes k = rhs(u) like ldg_rhs for the mesh and physics in cfg, with u
+ * Computes k = rhs(u) in FP64 like ldg_rhs for the mesh and physics in cfg
+ * (cfg->precision must be LDG_FP64: LDG_MIXED_F32X2 returns
+ * LDG_ERR_UNSUPPORTED, any other value LDG_ERR_INVALID), with u
  * and k DEVICE pointers in the reference layout (dofs, 5, nElements) on
  * device cfg->device; work is enqueued on `stream` (a cudaStream_t; NULL =
  * the legacy default stream) and the call returns without synchronising.

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/ldg.h"
@@ -401,16 +402,35 @@ cudaError_t harvest_times(ldg_solver* s) {
   return cudaSuccess;
 }
 
-__global__ void k_fp64_chain(double* out, int iters) {
-  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
-  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+// FP64 FMA throughput probe: 16 independent FMA chains per thread (enough
+// to cover the FMA latency at full occupancy), the loop unrolled so that
+// its counter and branch are a small share of the issue slots.  Thread 0
+// of each block records the block's SM cycle count (clock64), which gives
+// the FMA rate per SM per clock independently of the clock frequency.
+__global__ void __launch_bounds__(256) k_fp64_chain(double* out, long long* cycles, int* smid, int iters) {
+  double a[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) a[k] = threadIdx.x * 1e-9 + k * 1e-9;
   const double m = 0.999999999, c = 1e-12;
+  __syncthreads();
+  const long long t0 = clock64();
+#pragma unroll 4
   for (int i = 0; i < iters; ++i) {
-    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
-    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = fma(a[k], m, c);
   }
-  double r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
-  if (r == 1234.5) out[0] = r;  // keeps the chain live; never true
+  __syncthreads();
+  const long long t1 = clock64();
+  double r = 0.0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) r += a[k];
+  if (r == 1234.5) out[0] = r;  // keeps the chains live; never true
+  if (threadIdx.x == 0) {
+    unsigned sm;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+    cycles[blockIdx.x] = t1 - t0;
+    smid[blockIdx.x] = (int)sm;
+  }
 }
 
 // Stage kernels in the solver's arithmetic (mixed: FP32 pairs) or FP64.
@@ -973,18 +993,13 @@ int ldg_step(ldg_solver* s, int nsteps) {
       c.Uacc = s->Uacc;
       c.Unext = (stage < 3 || mixed) ? (void*)s->Us : nullptr;
       c.Tu_out = Tu_out;
-      c.diag = (stage == 3 && !mixed) ? s->diag : nullptr;
+      c.diag = stage == 3 ? s->diag : nullptr;
       c.flag = s->cfg.check_finite ? s->flag : nullptr;
       c.cacc = s->dt * kRkB[stage];
       c.cnext = stage < 3 ? s->dt * kRkA[stage] : 0.0;
       c.stage = stage;
       LDG_CUDA(tic(s, 1));
       LDG_CUDA(s_rhs(s, mixed, c));
-      LDG_CUDA(toc(s));
-    }
-    if (mixed) {  // computeKE of the new FP64 state
-      LDG_CUDA(tic(s, 2));
-      LDG_CUDA(d_ke(s->N, s->Uacc, s->diag, s->ops, s->stream));
       LDG_CUDA(toc(s));
     }
     // After four stages Tu[cur] holds the traces of Uacc = u^{n+1}.
@@ -1115,7 +1130,7 @@ int ldg_kernel_times(ldg_solver* s, double* ms, long long* launches, int max_cla
   return LDG_OK;
 }
 
-int ldg_probe_fp64_peak(int device, double* tflops) {
+int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* sm_mhz) {
   if (!tflops) return fail(LDG_ERR_INVALID, "null output");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -1125,27 +1140,64 @@ int ldg_probe_fp64_peak(int device, double* tflops) {
   LDG_CUDA(cudaSetDevice(device));
   int sms = 0;
   LDG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  // exactly one wave: as many 256-thread blocks per SM as fit
+  int per_sm = 0;
+  LDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fp64_chain, 256, 0));
+  if (per_sm < 1) return fail(LDG_ERR_CUDA, "probe kernel does not fit an SM");
+  const int blocks = sms * per_sm, threads = 256, iters = 2048;
   double* out = nullptr;
+  long long* cyc = nullptr;
+  int* smid = nullptr;
   LDG_CUDA(cudaMalloc((void**)&out, sizeof(double)));
+  if (cudaMalloc((void**)&cyc, sizeof(long long) * blocks) != cudaSuccess ||
+      cudaMalloc((void**)&smid, sizeof(int) * blocks) != cudaSuccess) {
+    cudaFree(out);
+    cudaFree(cyc);
+    return fail(LDG_ERR_NOMEM, "probe buffer");
+  }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int blocks = sms * 8, threads = 256, iters = 4096;
-  k_fp64_chain<<<blocks, threads>>>(out, iters);  // warm-up
+  k_fp64_chain<<<blocks, threads>>>(out, cyc, smid, iters);  // warm-up
   cudaEventRecord(e0);
-  k_fp64_chain<<<blocks, threads>>>(out, iters);
+  k_fp64_chain<<<blocks, threads>>>(out, cyc, smid, iters);
   cudaEventRecord(e1);
   cudaError_t err = cudaEventSynchronize(e1);
   float ms = 0.f;
   if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+  std::vector<long long> hc(blocks);
+  std::vector<int> hs(blocks);
+  if (err == cudaSuccess) err = cudaMemcpy(hc.data(), cyc, sizeof(long long) * blocks, cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess) err = cudaMemcpy(hs.data(), smid, sizeof(int) * blocks, cudaMemcpyDeviceToHost);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(out);
+  cudaFree(cyc);
+  cudaFree(smid);
   if (err != cudaSuccess) return fail(LDG_ERR_CUDA, cudaGetErrorString(err));
-  const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
-  *tflops = flops / (ms * 1e-3) / 1e12;
+  const double fmas_per_block = 16.0 * iters * threads;
+  *tflops = 2.0 * fmas_per_block * blocks / (ms * 1e-3) / 1e12;
+  // Per SM: the FMAs of the blocks it ran over the longest of their spans
+  // (one wave, so they ran side by side); the median over SMs.
+  std::vector<long long> span(1024, 0);
+  std::vector<int> count(1024, 0);
+  long long mx = 1;
+  for (int b = 0; b < blocks; ++b) {
+    const int id = hs[b] & 1023;
+    span[id] = std::max(span[id], hc[b]);
+    count[id] += 1;
+    mx = std::max(mx, hc[b]);
+  }
+  std::vector<double> rate;
+  for (int id = 0; id < 1024; ++id)
+    if (count[id]) rate.push_back(count[id] * fmas_per_block / (double)span[id]);
+  std::sort(rate.begin(), rate.end());
+  if (fma_per_sm_clk) *fma_per_sm_clk = rate.empty() ? 0.0 : rate[rate.size() / 2];
+  if (sm_mhz) *sm_mhz = (double)mx / (ms * 1e-3) / 1e6;
   return LDG_OK;
 }
+
+int ldg_probe_fp64_peak(int device, double* tflops) { return ldg_probe_fp64(device, tflops, nullptr, nullptr); }
 
 int ldg_save_checkpoint(ldg_solver* s, const char* path) {
   if (!s || !path || !*path) return fail(LDG_ERR_INVALID, "ldg_save_checkpoint: null solver or empty path");

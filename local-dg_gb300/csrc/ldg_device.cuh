@@ -50,6 +50,7 @@ struct OpsT {
   // RHS lifts.
   T As[3][kDevMaxN * kDevMaxN];
   T Lps[3][kDevMaxN], Lms[3][kDevMaxN];
+  T Bi[kDevMaxN * kDevMaxN];  // Gauss -> CGL nodal (the KE quirk), Bi[i*N + q]
   T g1, hg1, gamma, inv_re, kappa, two3, one;
 };
 
@@ -72,6 +73,7 @@ inline OpsT<T> make_opst(const DevOps& d, int N) {
       o.Lms[l][i] = host_cast(d.Lm[i] * d.ia[l], tag);
     }
   }
+  for (int i = 0; i < kDevMaxN * kDevMaxN; ++i) o.Bi[i] = host_cast(i < N * N ? d.Bi[i] : 0.0, tag);
   o.g1 = host_cast(d.g1, tag);
   o.hg1 = host_cast(0.5 * d.g1, tag);
   o.gamma = host_cast(d.gamma, tag);

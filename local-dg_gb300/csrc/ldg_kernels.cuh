@@ -306,51 +306,68 @@ __global__ void __launch_bounds__(Cfg<N>::T, Cfg<N>::T == 256 ? 4 : 1) k_grad(co
 }
 
 // ---------------------------------------------------------------------------
-// Kinetic energy of an FP64 state held in shared memory (sU: EPC*5*n Gauss
-// values; scr: EPC*8*n scratch).  Per element: diag[2e] = computeKE exactly
-// as the reference evaluates it (nodal values weighted by the Gauss weights,
-// solver.cpp:1021-1024, nodal values recovered with Bi (x) Bi (x) Bi), and
-// diag[2e+1] = the Gauss-quadrature kinetic energy.  Fixed-order sums.
-template <int N, int E = DefEPC<N>::value>
-__device__ __forceinline__ void ke_tail(const double* sU, double* scr, int ne, long e0, double* diag,
-                                        const DevOps& ops) {
+// Kinetic energy of a state held in shared memory (sU: EPC*5*n Gauss values
+// in the arithmetic type T; scr: EPC*8*n scratch of T).  Per element:
+// diag[2e] = computeKE exactly as the reference evaluates it (nodal values
+// weighted by the Gauss weights, solver.cpp:1021-1024, nodal values
+// recovered with Bi (x) Bi (x) Bi), and diag[2e+1] = the Gauss-quadrature
+// kinetic energy.  On the FP64 path every operation is FP64; on the mixed
+// path (T = dd, the FP32-pair copy of the new FP64 state) the nodal
+// transform and the point densities run in FP32-pair arithmetic and the
+// weights, the densities' products with them and the per-element sums in
+// FP64.  Fixed-order sums.
+template <int N, class T = double, int E = DefEPC<N>::value>
+__device__ __forceinline__ void ke_tail(const T* sU, T* scr, int ne, long e0, double* diag, const DevOps& ops,
+                                        const OpsT<T>& o) {
   constexpr int n = Cfg<N, E>::n, EPC = Cfg<N, E>::EPC;
-  double* s1 = scr;                 // EPC*4*n
-  double* s2 = scr + EPC * 4 * n;   // EPC*4*n
+  static_assert(sizeof(T) == sizeof(double), "8-byte values");
+  T* s1 = scr;                 // EPC*4*n
+  T* s2 = scr + EPC * 4 * n;   // EPC*4*n
   const int es = threadIdx.x / n, q = threadIdx.x % n;
   const bool act = es < ne;
   const int c[3] = {q % N, (q / N) % N, q / (N * N)};
 #pragma unroll
   for (int l = 0; l < 3; ++l) {
-    const double* sin = l == 0 ? sU : (l == 1 ? s1 : s2);
-    double* sout = l == 1 ? s2 : s1;
+    const T* sin = l == 0 ? sU : (l == 1 ? s1 : s2);
+    T* sout = l == 1 ? s2 : s1;
     const int instride = l == 0 ? kNS : 4;
     if (act) {
       const int st = stride_of<N>(l);
       const int b = q - c[l] * st;
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const double* row = sin + (es * instride + v) * n + b;
-        double acc = 0.0;
+        const T* row = sin + (es * instride + v) * n + b;
+        T acc{};
 #pragma unroll
-        for (int r = 0; r < N; ++r) acc = fma(ops.Bi[c[l] * N + r], row[r * st], acc);
+        for (int r = 0; r < N; ++r) {
+          if constexpr (std::is_same<T, double>::value) acc = fma(ops.Bi[c[l] * N + r], row[r * st], acc);
+          else acc = fma(o.Bi[c[l] * N + r], row[r * st], acc);
+        }
         sout[(es * 4 + v) * n + q] = acc;
       }
     }
     __syncthreads();
   }
+  double* d2 = reinterpret_cast<double*>(s2);
   if (act) {
-    const double* un = s1 + es * 4 * n + q;    // nodal rho, m at node index q
-    const double* ug = sU + es * kNS * n + q;  // Gauss values at point q
+    const T* un = s1 + es * 4 * n + q;    // nodal rho, m at node index q
+    const T* ug = sU + es * kNS * n + q;  // Gauss values at point q
     const double w3 = ops.w[c[0]] * ops.w[c[1]] * ops.w[c[2]];
-    s2[es * 2 * n + q] =
-        ops.J * w3 * (un[n] * un[n] + un[2 * n] * un[2 * n] + un[3 * n] * un[3 * n]) / (2 * un[0]);
-    s2[(es * 2 + 1) * n + q] =
-        ops.J * w3 * (ug[n] * ug[n] + ug[2 * n] * ug[2 * n] + ug[3 * n] * ug[3 * n]) / (2 * ug[0]);
+    if constexpr (std::is_same<T, double>::value) {
+      d2[es * 2 * n + q] =
+          ops.J * w3 * (un[n] * un[n] + un[2 * n] * un[2 * n] + un[3 * n] * un[3 * n]) / (2 * un[0]);
+      d2[(es * 2 + 1) * n + q] =
+          ops.J * w3 * (ug[n] * ug[n] + ug[2 * n] * ug[2 * n] + ug[3 * n] * ug[3 * n]) / (2 * ug[0]);
+    } else {
+      const T kn = (un[n] * un[n] + un[2 * n] * un[2 * n] + un[3 * n] * un[3 * n]) * rcp(un[0] + un[0]);
+      const T kg = (ug[n] * ug[n] + ug[2 * n] * ug[2 * n] + ug[3 * n] * ug[3 * n]) * rcp(ug[0] + ug[0]);
+      d2[es * 2 * n + q] = ops.J * w3 * Real<T>::to_f64(kn);
+      d2[(es * 2 + 1) * n + q] = ops.J * w3 * Real<T>::to_f64(kg);
+    }
   }
   __syncthreads();
   if (threadIdx.x < 2 * ne) {
-    const double* src = s2 + threadIdx.x * n;
+    const double* src = d2 + threadIdx.x * n;
     double acc = 0.0;
     for (int k = 0; k < n; ++k) acc += src[k];
     diag[(e0 + (threadIdx.x >> 1)) * 2 + (threadIdx.x & 1)] = acc;
@@ -366,7 +383,7 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_ke(const double* __restrict__ U, 
   const int ne = (int)min((long)EPC, ops.nE - e0);
   for (int i = threadIdx.x; i < ne * kNS * n; i += T) smem[i] = U[e0 * kNS * n + i];
   __syncthreads();
-  ke_tail<N>(smem, smem + EPC * kNS * n, ne, e0, diag, ops);
+  ke_tail<N, double>(smem, smem + EPC * kNS * n, ne, e0, diag, ops, OpsT<double>{});
 }
 
 // ---------------------------------------------------------------------------
@@ -534,18 +551,16 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
   __syncthreads();
   // 5. traces of the next stage input for the face fluxes of the next pass
   write_traces<N, T, E>(sU, ne, e0, a.Tu_out, o);
-  // 6. diagnostics on the new state (last stage of the FP64 path; the mixed
-  //    path runs k_ke on the FP64 state instead)
-  if constexpr (std::is_same<T, double>::value) {
-    if (a.stage == 3 && a.diag) {
-      __syncthreads();
-      ke_tail<N, E>(sU, sF + EPC * kNS * n, ne, e0, a.diag, ops);
-    }
+  // 6. diagnostics on the new state (last stage; on the mixed path from
+  //    the FP32-pair copy of the new FP64 state)
+  if (a.stage == 3 && a.diag) {
+    __syncthreads();
+    ke_tail<N, T, E>(sU, sF + EPC * kNS * n, ne, e0, a.diag, ops, o);
   }
 }
 
 template <int N, class T>
-__global__ void __launch_bounds__(Cfg<N>::T) k_rhs(const __grid_constant__ StageArgs<T> a,
+__global__ void __launch_bounds__(Cfg<N>::T, Cfg<N>::T == 256 ? 4 : 1) k_rhs(const __grid_constant__ StageArgs<T> a,
                                                    const __grid_constant__ DevOps ops,
                                                    const __grid_constant__ OpsT<T> o) {
   extern __shared__ double smem_raw[];

@@ -119,6 +119,10 @@ extern "C" int ldg_rhs_noalloc(const ldg_config* cfg, const double* u, double* k
   if (!(c.Re > 0) || !(c.Pr > 0) || !(c.gamma > 1) || !(c.L > 0))
     return fail(LDG_ERR_INVALID, "ldg_rhs_noalloc: physical parameters must be positive (gamma > 1)");
   if (c.device < 0 || c.device >= kMaxDevices) return fail(LDG_ERR_INVALID, "ldg_rhs_noalloc: bad device");
+  if (c.precision != LDG_FP64 && c.precision != LDG_MIXED_F32X2)
+    return fail(LDG_ERR_INVALID, "ldg_rhs_noalloc: precision must be LDG_FP64 or LDG_MIXED_F32X2");
+  if (c.precision != LDG_FP64)
+    return fail(LDG_ERR_UNSUPPORTED, "ldg_rhs_noalloc: computes in FP64 only (precision LDG_FP64)");
   const int N = c.p + 1, n = N * N * N, nf = N * N;
   const long long nE = (long long)c.nx * c.ny * c.nz;
   const long long need = nE * (long long)(kNS * n + 6 * kNS * nf + kNQ * n + 3 * kNQ * nf + 3 * kNS * nf);

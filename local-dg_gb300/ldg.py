@@ -144,6 +144,7 @@ SIGNATURES = {
     "ldg_enable_kernel_timing": (_i, [_vp, _i]),
     "ldg_kernel_times": (_i, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _i, _i]),
     "ldg_probe_fp64_peak": (_i, [_i, _dp]),
+    "ldg_probe_fp64": (_i, [_i, _dp, _dp, _dp]),
     "ldg_rhs_noalloc": (_i, [ctypes.POINTER(LdgConfig), _vp, _vp, _vp]),
     "ldg_ensemble_create": (_i, [ctypes.POINTER(LdgConfig), _i, ctypes.POINTER(_vp)]),
     "ldg_ensemble_destroy": (_i, [_vp]),
@@ -202,6 +203,14 @@ def probe_fp64_peak(device: int = 0) -> float:
     out = ctypes.c_double()
     _check(load().ldg_probe_fp64_peak(device, ctypes.byref(out)), "ldg_probe_fp64_peak")
     return out.value
+
+
+def probe_fp64(device: int = 0) -> dict:
+    """The FP64 probe's readings: TFLOP/s, FMAs per SM per clock and the SM
+    clock (MHz) it ran at."""
+    t, r, m = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _check(load().ldg_probe_fp64(device, ctypes.byref(t), ctypes.byref(r), ctypes.byref(m)), "ldg_probe_fp64")
+    return {"tflops": t.value, "fma_per_sm_clk": r.value, "sm_mhz": m.value}
 
 
 class LdgError(RuntimeError):

@@ -65,6 +65,11 @@ typedef struct ldgo {
   int *eToE;        /* 6 x nE, periodic neighbour (ghost slots resolved) */
   /* work arrays (solver.cpp:318-325) */
   double *uCurr, *uInterp2D, *uInterp3D, *ks, *Dus, *DuInterp2D, *DuInterp3D, *onFaces, *flx;
+  /* 1-D factors (N x N, row-major out x in) of the dense operators above;
+   * on a uniform hex mesh every one of them is a Kronecker product of
+   * these (see ldgo_set_factored). */
+  double I1[64], IWt[64], DWt[64], M1[64], S1[64], M1i[64];
+  int factored;
   /* optional OpenBLAS */
   void *blas;
   dgemm_fn dgemm;
@@ -334,6 +339,59 @@ static void face_map(int m, int* ef) {
 
 /* ----------------------------------------------------------------- setup */
 
+/* 1-D factors of the reference operators.  The basis is the tensor product
+ * of the 1-D Lagrange polynomials l_a on the CGL nodes (the reference builds
+ * it as Legendre modes times the inverse Vandermonde, dgMath.cpp:545-615),
+ * and the quadrature is the tensor Gauss rule, so on a uniform hex
+ * (constant diagonal Jacobian) every dense operator of solver.cpp:74-192 is
+ * a Kronecker product of
+ *   I1[q][a]  = l_a(x_q)                      (Interp3D = I1^3, Interp2D = I1^2)
+ *   IWt[a][q] = l_a(x_q) w_q                  (Kels_l, Kels2D_l: test side)
+ *   DWt[a][q] = l_a'(x_q) w_q                 (Kels_l along l)
+ *   M1 = I1^T W I1                            (Mel = J M1^3)
+ *   S1 = D1^T W I1                            (Sels_l = J/alpha_l S1 (x) M1 (x) M1, S1 along l)
+ * with M1i = M1^-1.  Row-major out x in. */
+static void setup_factors(ldgo* o, const double* cheb, const double* xq, const double* wq) {
+  int p = o->p, N = p + 1;
+  double P[64], Pq[64], dPq[64], C[64], D1[64];
+  legendre(p, N, cheb, P, NULL);
+  legendre(p, N, xq, Pq, dPq);
+  for (int i = 0; i < N * N; ++i) C[i] = 0.0;
+  for (int i = 0; i < N; ++i) C[i + i * N] = 1.0;
+  lu_solve(N, P, N, C); /* C = inverse Vandermonde, column-major */
+  for (int q = 0; q < N; ++q)
+    for (int a = 0; a < N; ++a) {
+      double v = 0.0, d = 0.0;
+      for (int m = 0; m < N; ++m) {
+        v += Pq[q + m * N] * C[m + a * N];
+        d += dPq[q + m * N] * C[m + a * N];
+      }
+      o->I1[q * N + a] = v;
+      D1[q * N + a] = d;
+    }
+  for (int a = 0; a < N; ++a)
+    for (int q = 0; q < N; ++q) {
+      o->IWt[a * N + q] = o->I1[q * N + a] * wq[q];
+      o->DWt[a * N + q] = D1[q * N + a] * wq[q];
+    }
+  for (int a = 0; a < N; ++a)
+    for (int b = 0; b < N; ++b) {
+      double m = 0.0, sd = 0.0;
+      for (int q = 0; q < N; ++q) {
+        m += o->I1[q * N + a] * wq[q] * o->I1[q * N + b];
+        sd += D1[q * N + a] * wq[q] * o->I1[q * N + b];
+      }
+      o->M1[a * N + b] = m;
+      o->S1[a * N + b] = sd;
+    }
+  double Mc[64], Mi[64];
+  for (int a = 0; a < N; ++a)
+    for (int b = 0; b < N; ++b) { Mc[a + b * N] = o->M1[a * N + b]; Mi[a + b * N] = a == b; }
+  lu_solve(N, Mc, N, Mi);
+  for (int a = 0; a < N; ++a)
+    for (int b = 0; b < N; ++b) o->M1i[a * N + b] = Mi[a + b * N];
+}
+
 void ldgo_destroy(ldgo* o);
 
 static int ldgo_setup(ldgo* o) {
@@ -397,6 +455,7 @@ static int ldgo_setup(ldgo* o) {
         o->Kels2D[q + i * nf + l * nf * nf] = o->Interp2D[q + i * nf] * w2[q] * scaleL;
   }
   free(l3D); free(coeffs); free(polyQ); free(dpolyQ); free(phiQ); free(dphiQ);
+  setup_factors(o, cheb, xq, wq);
   /* Mesh connectivity (mesh.cpp:201-353): periodic neighbours directly. */
   o->efToN = (int*)malloc(sizeof(int) * nf * NF);
   face_map(N, o->efToN);
@@ -674,21 +733,23 @@ static void flux_roe(const double* uN, const double* uK, const double* nrm, doub
 /* Gather face nodes and interpolate to face/volume quadrature points
  * (solver.cpp:541-577); periodic neighbours replace the ghost exchange
  * (solver.cpp:929-998). dim = 1 (u) or 3 (Du). */
-static void interpolate(ldgo* o, const double* curr, double* i2d, double* i3d, int dim) {
+static void interpolate(ldgo* o, const double* curr, double* i2d, double* i3d, int dim, long e0, long e1) {
   int n = o->n, nf = o->nf, nE = o->nE;
-  long blk = (long)nf * NS * NF * nE;
+  long blk = (long)nf * NS * NF * nE, nU = (long)n * NS * nE, ne = e1 - e0;
   for (int l = 0; l < dim; ++l) {
     long k;
 #pragma omp parallel for schedule(static)
-    for (k = 0; k < nE; ++k)
+    for (k = e0; k < e1; ++k)
       for (int f = 0; f < NF; ++f)
         for (int s = 0; s < NS; ++s)
           for (int j = 0; j < nf; ++j)
             o->onFaces[j + nf * (s + NS * (f + NF * k)) + l * blk] =
-                curr[o->efToN[j + nf * f] + n * (s + NS * k) + (long)l * n * NS * nE];
-    gemm(o, 0, nf, NS * NF * nE, nf, 1.0, o->Interp2D, nf, o->onFaces + l * blk, nf, 0.0, i2d + l * blk, nf);
+                curr[o->efToN[j + nf * f] + n * (s + NS * k) + (long)l * nU];
+    long off = (long)nf * NS * NF * e0 + l * blk;
+    gemm(o, 0, nf, (int)(NS * NF * ne), nf, 1.0, o->Interp2D, nf, o->onFaces + off, nf, 0.0, i2d + off, nf);
+    long voff = (long)n * NS * e0 + l * nU;
+    gemm(o, 0, n, (int)(NS * ne), n, 1.0, o->Interp3D, n, curr + voff, n, 0.0, i3d + voff, n);
   }
-  gemm(o, 0, n, NS * nE * dim, n, 1.0, o->Interp3D, n, curr, n, 0.0, i3d, n);
 }
 
 /* Adds Kels2D(:,:,f/2)^T * fstar into the face nodes of res (the per-face
@@ -706,17 +767,264 @@ static void face_lift(const ldgo* o, int f, const double* fstar, double* res) {
 
 static const double kNormals[NF][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
 
+/* ------------------------------------------------- sum-factorised RHS */
+
+/* out = (A2 (x) A1 (x) A0) in on an N^3 block, index a + N b + N^2 c, each
+ * A row-major N x N (out x in): three 1-D passes, x then y then z. */
+static inline __attribute__((always_inline)) void apply3_n(const int N, const double* A0, const double* A1,
+                                                           const double* A2, const double* in, double* out) {
+  double t1[512], t2[512];
+  int N2 = N * N;
+  for (int c = 0; c < N; ++c)
+    for (int b = 0; b < N; ++b)
+      for (int a = 0; a < N; ++a) {
+        double acc = 0.0;
+        for (int r = 0; r < N; ++r) acc += A0[a * N + r] * in[r + N * b + N2 * c];
+        t1[a + N * b + N2 * c] = acc;
+      }
+  for (int c = 0; c < N; ++c)
+    for (int b = 0; b < N; ++b)
+      for (int a = 0; a < N; ++a) {
+        double acc = 0.0;
+        for (int r = 0; r < N; ++r) acc += A1[b * N + r] * t1[a + N * r + N2 * c];
+        t2[a + N * b + N2 * c] = acc;
+      }
+  for (int c = 0; c < N; ++c)
+    for (int b = 0; b < N; ++b)
+      for (int a = 0; a < N; ++a) {
+        double acc = 0.0;
+        for (int r = 0; r < N; ++r) acc += A2[c * N + r] * t2[a + N * b + N2 * r];
+        out[a + N * b + N2 * c] = acc;
+      }
+}
+
+/* apply3_n with N a compile-time constant for the common orders, so the
+ * 1-D loops unroll. */
+static void apply3(int N, const double* A0, const double* A1, const double* A2, const double* in, double* out) {
+  switch (N) {
+    case 2: apply3_n(2, A0, A1, A2, in, out); return;
+    case 3: apply3_n(3, A0, A1, A2, in, out); return;
+    case 4: apply3_n(4, A0, A1, A2, in, out); return;
+    case 5: apply3_n(5, A0, A1, A2, in, out); return;
+    case 6: apply3_n(6, A0, A1, A2, in, out); return;
+    default: apply3_n(N, A0, A1, A2, in, out); return;
+  }
+}
+
+/* out = (A1 (x) A0) in on an N^2 face block, index a + N b. */
+static inline __attribute__((always_inline)) void apply2_n(const int N, const double* A0, const double* A1,
+                                                           const double* in, double* out) {
+  double t1[64];
+  for (int b = 0; b < N; ++b)
+    for (int a = 0; a < N; ++a) {
+      double acc = 0.0;
+      for (int r = 0; r < N; ++r) acc += A0[a * N + r] * in[r + N * b];
+      t1[a + N * b] = acc;
+    }
+  for (int b = 0; b < N; ++b)
+    for (int a = 0; a < N; ++a) {
+      double acc = 0.0;
+      for (int r = 0; r < N; ++r) acc += A1[b * N + r] * t1[a + N * r];
+      out[a + N * b] = acc;
+    }
+}
+
+static void apply2(int N, const double* A0, const double* A1, const double* in, double* out) {
+  switch (N) {
+    case 2: apply2_n(2, A0, A1, in, out); return;
+    case 3: apply2_n(3, A0, A1, in, out); return;
+    case 4: apply2_n(4, A0, A1, in, out); return;
+    case 5: apply2_n(5, A0, A1, in, out); return;
+    case 6: apply2_n(6, A0, A1, in, out); return;
+    default: apply2_n(N, A0, A1, in, out); return;
+  }
+}
+
+/* Interp3D / Interp2D applications of interpolate() (solver.cpp:541-577)
+ * in factored form: volume values I1^3 u and face values I1^2 u|face for
+ * dim consecutive fields of (n,5,nE) each. */
+static void interpolate_factored(ldgo* o, const double* curr, double* i2d, double* i3d, int dim) {
+  int N = o->N, n = o->n, nf = o->nf, nE = o->nE;
+  long nU = (long)n * NS * nE, blk = (long)nf * NS * NF * nE;
+  for (int l = 0; l < dim; ++l) {
+    long e;
+#pragma omp parallel for schedule(static)
+    for (e = 0; e < nE; ++e) {
+      double face[64];
+      for (int s = 0; s < NS; ++s) {
+        const double* ue = curr + l * nU + (long)n * (s + NS * e);
+        apply3(N, o->I1, o->I1, o->I1, ue, i3d + l * nU + (long)n * (s + NS * e));
+        for (int f = 0; f < NF; ++f) {
+          for (int j = 0; j < nf; ++j) face[j] = ue[o->efToN[j + nf * f]];
+          apply2(N, o->I1, o->I1, face, i2d + l * blk + nf * (s + NS * (f + NF * e)));
+        }
+      }
+    }
+  }
+}
+
+/* Kels2D(:,:,f/2)^T fstar scattered to the face nodes (face_lift) as
+ * J/alpha_l (IWt (x) IWt) fstar. */
+static void face_lift_factored(const ldgo* o, int f, const double* fstar, double* res) {
+  int N = o->N, n = o->n, nf = o->nf;
+  double scaleL = o->J / o->alpha[f / 2], out[64];
+  for (int s = 0; s < NS; ++s) {
+    apply2(N, o->IWt, o->IWt, fstar + nf * s, out);
+    for (int j = 0; j < nf; ++j) res[o->efToN[j + nf * f] + n * s] += scaleL * out[j];
+  }
+}
+
+/* Mel \ x for one element's 5 blocks: (1/J) M1i^3 x, in place. */
+static void mass_solve_factored(const ldgo* o, double* x) {
+  int N = o->N, n = o->n;
+  double tmp[512];
+  for (int s = 0; s < NS; ++s) {
+    apply3(N, o->M1i, o->M1i, o->M1i, x + n * s, tmp);
+    for (int i = 0; i < n; ++i) x[i + n * s] = tmp[i] / o->J;
+  }
+}
+
+/* The gradient half of rk4Rhs (solver.cpp:495-508) in factored form:
+ * Dus_l = Mel \ (F_l(u) - Sels_l u), with uInterp2D/uInterp3D of uCurr
+ * already computed. */
+static void gradient_factored(ldgo* o, const double* uCurr) {
+  int N = o->N, n = o->n, nf = o->nf, nE = o->nE;
+  long nU = (long)n * NS * nE;
+  long e;
+#pragma omp parallel for schedule(static)
+  for (e = 0; e < nE; ++e) {
+    double fstar[NS * 64], tmp[512];
+    for (int l = 0; l < DIM; ++l) {
+      double* D = o->Dus + l * nU + (long)e * n * NS;
+      for (int i = 0; i < n * NS; ++i) D[i] = 0.0;
+      for (int f = 0; f < NF; ++f) { /* localDGFlux (solver.cpp:585-635) */
+        int nK = o->eToE[f + NF * e], nF = f ^ 1;
+        double nl = kNormals[f][l];
+        for (int s = 0; s < NS; ++s)
+          for (int q = 0; q < nf; ++q) {
+            double uK = o->uInterp2D[q + nf * (s + NS * (f + NF * e))];
+            double uN = o->uInterp2D[q + nf * (s + NS * (nF + NF * (long)nK))];
+            fstar[q + nf * s] = ((nl > 0) ? uK : uN) * nl; /* numericalFluxL */
+          }
+        face_lift_factored(o, f, fstar, D);
+      }
+      const double* A[3] = {o->M1, o->M1, o->M1};
+      A[l] = o->S1;
+      double scaleL = o->J / o->alpha[l];
+      for (int s = 0; s < NS; ++s) { /* -Sels_l u, solver.cpp:500 */
+        apply3(N, A[0], A[1], A[2], uCurr + (long)n * (s + NS * e), tmp);
+        for (int i = 0; i < n; ++i) D[i + n * s] += -scaleL * tmp[i];
+      }
+      mass_solve_factored(o, D);
+    }
+  }
+}
+
+/* rk4Rhs (solver.cpp:486-535) with every dense operator applied in its
+ * Kronecker-factored form: the same discrete operator and the same flux
+ * functions, O(N^4) instead of O(N^6) work per element and variable. */
+static void rhs_factored(ldgo* o, const double* uCurr, double* k) {
+  int N = o->N, n = o->n, nf = o->nf, nE = o->nE;
+  long nU = (long)n * NS * nE;
+  long fblk = (long)nf * NS * NF * nE;
+  interpolate_factored(o, uCurr, o->uInterp2D, o->uInterp3D, 1);
+  gradient_factored(o, uCurr);
+  interpolate_factored(o, o->Dus, o->DuInterp2D, o->DuInterp3D, DIM);
+  long e;
+#pragma omp parallel for schedule(static)
+  for (e = 0; e < nE; ++e) {
+    double fstar[NS * 64], fl[NS], uK[NS], uN[NS], DuK[NS * DIM], DuN[NS * DIM], Fv[NS * DIM];
+    double flx[DIM][NS][512], tmp[512];
+    double* ke = k + (long)e * n * NS;
+    for (int i = 0; i < n * NS; ++i) ke[i] = 0.0;
+    for (int f = 0; f < NF; ++f) { /* convectDGFlux (solver.cpp:643-698) */
+      int nK = o->eToE[f + NF * e], nF = f ^ 1;
+      for (int q = 0; q < nf; ++q) {
+        for (int s = 0; s < NS; ++s) {
+          uK[s] = o->uInterp2D[q + nf * (s + NS * (f + NF * e))];
+          uN[s] = o->uInterp2D[q + nf * (s + NS * (nF + NF * (long)nK))];
+        }
+        flux_roe(uN, uK, kNormals[f], fl);
+        for (int s = 0; s < NS; ++s) fstar[q + nf * s] = fl[s];
+      }
+      face_lift_factored(o, f, fstar, ke);
+    }
+    for (int f = 0; f < NF; ++f) { /* viscousDGFlux (solver.cpp:750-814) */
+      int nK = o->eToE[f + NF * e], nF = f ^ 1;
+      const double* nrm = kNormals[f];
+      int kWins = (nrm[0] + nrm[1] + nrm[2]) > 0; /* numericalFluxV */
+      for (int q = 0; q < nf; ++q) {
+        for (int s = 0; s < NS; ++s) {
+          uK[s] = o->uInterp2D[q + nf * (s + NS * (f + NF * e))];
+          uN[s] = o->uInterp2D[q + nf * (s + NS * (nF + NF * (long)nK))];
+        }
+        for (int l = 0; l < DIM; ++l)
+          for (int s = 0; s < NS; ++s) {
+            DuK[s + NS * l] = o->DuInterp2D[q + nf * (s + NS * (f + NF * e)) + l * fblk];
+            DuN[s + NS * l] = o->DuInterp2D[q + nf * (s + NS * (nF + NF * (long)nK)) + l * fblk];
+          }
+        flux_v(o, uK, kWins ? DuN : DuK, Fv);
+        for (int s = 0; s < NS; ++s) {
+          double acc = 0.0;
+          for (int l = 0; l < DIM; ++l) acc -= Fv[s + NS * l] * nrm[l];
+          fstar[q + nf * s] = acc;
+        }
+      }
+      face_lift_factored(o, f, fstar, ke);
+    }
+    for (int i = 0; i < n * NS; ++i) ke[i] = -ke[i]; /* dscal -1 */
+    for (int q = 0; q < n; ++q) { /* volume fluxes (solver.cpp:701-741, 817-864) */
+      double u[NS], Du[NS * DIM], Fc[NS * DIM];
+      for (int s = 0; s < NS; ++s) u[s] = o->uInterp3D[q + n * (s + NS * e)];
+      for (int l = 0; l < DIM; ++l)
+        for (int s = 0; s < NS; ++s) Du[s + NS * l] = o->DuInterp3D[q + n * (s + NS * e) + l * nU];
+      flux_c(o, u, Fc);
+      flux_v(o, u, Du, Fv);
+      for (int l = 0; l < DIM; ++l)
+        for (int s = 0; s < NS; ++s) flx[l][s][q] = Fc[s + NS * l] - Fv[s + NS * l];
+    }
+    for (int l = 0; l < DIM; ++l) { /* Kels_l^T (fc - fv), solver.cpp:736-738, 859-861 */
+      const double* A[3] = {o->IWt, o->IWt, o->IWt};
+      A[l] = o->DWt;
+      double scaleL = o->J / o->alpha[l];
+      for (int s = 0; s < NS; ++s) {
+        apply3(N, A[0], A[1], A[2], flx[l][s], tmp);
+        for (int i = 0; i < n; ++i) ke[i + n * s] += scaleL * tmp[i];
+      }
+    }
+    mass_solve_factored(o, ke);
+  }
+}
+
+/* Switches a handle between the dense operator chain (0, the reference's
+ * GEMM structure) and the Kronecker-factored one (1).  Both evaluate the
+ * same discrete operator; they differ in rounding only.  The factored form
+ * makes long runs at the benchmark meshes affordable on a CPU. */
+void ldgo_set_factored(ldgo* o, int on) { o->factored = on ? 1 : 0; }
+
 /* One RHS evaluation k = rhs(uCurr) (rk4Rhs, solver.cpp:486-535). */
-void ldgo_rhs(ldgo* o, const double* uCurr, double* k) {
+/* rk4Rhs (solver.cpp:486-535) with the reference's dense operator chain,
+ * for the residual of elements [r0, r1).  The full mesh is r0 = 0, r1 =
+ * nE.  A z-slab of whole planes (r0, r1 multiples of nx*ny, at least two
+ * planes from either end of the numbering) needs the gradient one plane
+ * beyond it and the face values of u two planes beyond it; only those
+ * halos are evaluated, which makes a bounded sample of the workload of a
+ * large mesh.  k receives the slab's columns only. */
+static void rhs_dense(ldgo* o, const double* uCurr, double* k, long r0, long r1) {
   int n = o->n, nf = o->nf, nE = o->nE;
   long nU = (long)n * NS * nE;
   long fblk = (long)nf * NS * NF * nE;
-  interpolate(o, uCurr, o->uInterp2D, o->uInterp3D, 1);
+  long plane = (long)o->nx * o->ny;
+  long g0 = 0, g1 = nE, i0 = 0, i1 = nE; /* gradient and u-interpolation ranges */
+  if (!(r0 == 0 && r1 == nE)) {
+    g0 = r0 - plane; g1 = r1 + plane; i0 = r0 - 2 * plane; i1 = r1 + 2 * plane;
+  }
+  interpolate(o, uCurr, o->uInterp2D, o->uInterp3D, 1, i0, i1);
   /* Gradient pass: Dus_l = Mel \ (-S_l u + F_l(u))  (solver.cpp:495-508) */
-  memset(o->Dus, 0, sizeof(double) * nU * DIM);
   long e;
+  for (int l = 0; l < DIM; ++l) memset(o->Dus + l * nU + (long)n * NS * g0, 0, sizeof(double) * n * NS * (g1 - g0));
 #pragma omp parallel for schedule(static)
-  for (e = 0; e < nE; ++e) { /* localDGFlux (solver.cpp:585-635) */
+  for (e = g0; e < g1; ++e) { /* localDGFlux (solver.cpp:585-635) */
     double fstar[NS * 64];
     for (int l = 0; l < DIM; ++l)
       for (int f = 0; f < NF; ++f) {
@@ -731,15 +1039,18 @@ void ldgo_rhs(ldgo* o, const double* uCurr, double* k) {
         face_lift(o, f, fstar, o->Dus + l * nU + (long)e * n * NS);
       }
   }
+  long gc = (long)n * NS * g0;
   for (int l = 0; l < DIM; ++l) {
-    gemm(o, 0, n, NS * nE, n, -1.0, o->Sels + (long)l * n * n, n, uCurr, n, 1.0, o->Dus + l * nU, n);
-    mass_solve(o, o->Dus + l * nU, (long)NS * nE);
+    gemm(o, 0, n, (int)(NS * (g1 - g0)), n, -1.0, o->Sels + (long)l * n * n, n, uCurr + gc, n, 1.0,
+         o->Dus + l * nU + gc, n);
+    mass_solve(o, o->Dus + l * nU + gc, (long)NS * (g1 - g0));
   }
-  interpolate(o, o->Dus, o->DuInterp2D, o->DuInterp3D, DIM);
+  interpolate(o, o->Dus, o->DuInterp2D, o->DuInterp3D, DIM, g0, g1);
   /* Residual: faces, negate, volumes, mass solve (solver.cpp:516-533) */
-  memset(k, 0, sizeof(double) * nU);
+  long rc = (long)n * NS * r0;
+  memset(k + rc, 0, sizeof(double) * n * NS * (r1 - r0));
 #pragma omp parallel for schedule(static)
-  for (e = 0; e < nE; ++e) {
+  for (e = r0; e < r1; ++e) {
     double fstar[NS * 64];
     double uK[NS], uN[NS], DuK[NS * DIM], DuN[NS * DIM], fl[NS], Fv[NS * DIM];
     for (int f = 0; f < NF; ++f) { /* convectDGFlux (solver.cpp:643-698) */
@@ -792,8 +1103,29 @@ void ldgo_rhs(ldgo* o, const double* uCurr, double* k) {
     }
   }
   for (int l = 0; l < DIM; ++l)
-    gemm(o, 1, n, NS * nE, n, 1.0, o->Kels + (long)l * n * n, n, o->flx + l * nU, n, 1.0, k, n);
-  mass_solve(o, k, (long)NS * nE);
+    gemm(o, 1, n, (int)(NS * (r1 - r0)), n, 1.0, o->Kels + (long)l * n * n, n, o->flx + l * nU + rc, n, 1.0,
+         k + rc, n);
+  mass_solve(o, k + rc, (long)NS * (r1 - r0));
+}
+
+/* One RHS evaluation k = rhs(uCurr) (rk4Rhs, solver.cpp:486-535). */
+void ldgo_rhs(ldgo* o, const double* uCurr, double* k) {
+  if (o->factored) {
+    rhs_factored(o, uCurr, k);
+    return;
+  }
+  rhs_dense(o, uCurr, k, 0, o->nE);
+}
+
+/* One rk4Rhs stage restricted to the residual of the z-planes [z0, z0 +
+ * planes) with the dense chain (see rhs_dense): a bounded sample of the
+ * work of a full-mesh stage.  Needs 2 <= z0 and z0 + planes <= nz - 2.
+ * Returns 0, or -1 for a slab too close to the ends of the numbering. */
+int ldgo_rhs_slab(ldgo* o, const double* uCurr, double* k, int z0, int planes) {
+  if (z0 < 2 || planes < 1 || z0 + planes > o->nz - 2) return -1;
+  long plane = (long)o->nx * o->ny;
+  rhs_dense(o, uCurr, k, z0 * plane, (z0 + planes) * plane);
+  return 0;
 }
 
 /* Kinetic energy exactly as computeKE (solver.cpp:1007-1034): nodal values
@@ -808,6 +1140,43 @@ double ldgo_compute_ke(const ldgo* o, const double* u) {
       ke += o->J * o->wQ3[q] *
             (uk[q + n] * uk[q + n] + uk[q + 2 * n] * uk[q + 2 * n] + uk[q + 3 * n] * uk[q + 3 * n]) / (2 * uk[q]);
     total += ke;
+  }
+  return total / (o->rho0 * pow(2 * M_PI * o->L, 3.0));
+}
+
+/* Enstrophy of a state: the Gauss quadrature of rho |curl v|^2 / 2 from
+ * the LDG gradient Dus of u (the first half of rk4Rhs, solver.cpp:495-508)
+ * and the interpolants Interp3D u, Interp3D Dus, normalised like computeKE
+ * (solver.cpp:1007-1034) by rho0 (2 pi L)^3.  The reference prints no
+ * enstrophy; this is the functional the CUDA path reports, on the
+ * reference's own gradient. */
+double ldgo_enstrophy(ldgo* o, const double* u) {
+  int n = o->n, nE = o->nE;
+  long nU = (long)n * NS * nE;
+  if (o->factored) {
+    interpolate_factored(o, u, o->uInterp2D, o->uInterp3D, 1);
+    gradient_factored(o, u);
+    interpolate_factored(o, o->Dus, o->DuInterp2D, o->DuInterp3D, DIM);
+  } else {
+    double* k = (double*)malloc(sizeof(double) * nU);
+    ldgo_rhs(o, u, k); /* leaves uInterp3D, DuInterp3D of u behind */
+    free(k);
+  }
+  double total = 0.0;
+  long e;
+#pragma omp parallel for schedule(static) reduction(+ : total)
+  for (e = 0; e < nE; ++e) {
+    double el = 0.0;
+    for (int q = 0; q < n; ++q) {
+      double rho = o->uInterp3D[q + n * (NS * e)], v[3], G[3][3];
+      for (int i = 0; i < 3; ++i) v[i] = o->uInterp3D[q + n * (1 + i + NS * e)] / rho;
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i)
+          G[i][j] = (o->DuInterp3D[q + n * (1 + i + NS * e) + j * nU] - o->DuInterp3D[q + n * (NS * e) + j * nU] * v[i]) / rho;
+      double wx = G[2][1] - G[1][2], wy = G[0][2] - G[2][0], wz = G[1][0] - G[0][1];
+      el += o->J * o->wQ3[q] * 0.5 * rho * (wx * wx + wy * wy + wz * wz);
+    }
+    total += el;
   }
   return total / (o->rho0 * pow(2 * M_PI * o->L, 3.0));
 }

@@ -63,6 +63,11 @@ def lib():
         L.ldgo_step.argtypes = [vp, dp, i, dp]
         L.ldgo_compute_ke.restype = d
         L.ldgo_compute_ke.argtypes = [vp, dp]
+        L.ldgo_set_factored.argtypes = [vp, i]
+        L.ldgo_rhs_slab.restype = i
+        L.ldgo_rhs_slab.argtypes = [vp, dp, dp, i, i]
+        L.ldgo_enstrophy.restype = d
+        L.ldgo_enstrophy.argtypes = [vp, dp]
         L.ldgo_get_operator.restype = i
         L.ldgo_get_operator.argtypes = [vp, i, dp]
         _lib = L
@@ -152,6 +157,18 @@ class Oracle:
             _lib.ldgo_destroy(h)
             self._h = None
 
+    def set_factored(self, on: bool = True) -> None:
+        """Dense operator chain (the reference's GEMM structure) or the
+        Kronecker-factored one: the same discrete operator, different
+        rounding, O(N^4) instead of O(N^6) work per element."""
+        lib().ldgo_set_factored(self._h, 1 if on else 0)
+
+    def enstrophy(self, u: np.ndarray) -> float:
+        """rho |curl v|^2 / 2 integrated with the Gauss rule from the LDG
+        gradient of u, normalised like computeKE."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        return lib().ldgo_enstrophy(self._h, _ptr(u))
+
     def set_dt(self, dt: float) -> None:
         lib().ldgo_set_dt(self._h, dt)
         self.dt = dt
@@ -170,6 +187,14 @@ class Oracle:
         k = np.zeros(self.shape)
         lib().ldgo_rhs(self._h, _ptr(u), _ptr(k))
         return k
+
+    def rhs_slab(self, u: np.ndarray, k: np.ndarray, z0: int, planes: int) -> None:
+        """The dense RHS for the residual of z-planes [z0, z0+planes) only
+        (with the halo planes it needs), written into k's slab columns: a
+        bounded sample of a large mesh's stage work."""
+        assert u.shape == self.shape and k.shape == self.shape
+        if lib().ldgo_rhs_slab(self._h, _ptr(u), _ptr(k), z0, planes) != 0:
+            raise ValueError(f"slab z0={z0} planes={planes} does not fit nz={self.nx}")
 
     def step(self, u: np.ndarray, nsteps: int = 1):
         u = np.array(u, dtype=np.float64, order="C", copy=True)

@@ -19,14 +19,18 @@
  *   rhs  <nx> <p> <state_in|-> <outprefix> [threads]
  *        One rk4Rhs on the given state (or Taylor-Green), istage 0:
  *        writes <outprefix>.k (dofs,5,nE) and <outprefix>.u0.
- *   series <nx> <p> <steps> <outprefix> <index_file> [threads]
+ *   series <nx> <p> <steps> <outprefix> <index_file> [threads] [ens_every]
  *        Taylor-Green -> <steps> RK4 steps, recording after every step the
  *        KE (<outprefix>.ke), the sum of squares of each conserved
  *        variable over all nodes and elements (<outprefix>.norms,
  *        steps x 5) and the state entries at the flat column-major
  *        indices listed in <index_file> (int64) (<outprefix>.samples,
  *        steps x count).  For meshes whose full states are too large to
- *        keep for every step.
+ *        keep for every step.  With ens_every > 0, after every
+ *        ens_every-th step also the enstrophy of the state
+ *        (<outprefix>.enst: pairs step, value), from the reference's own
+ *        LDG gradient Dus of that state (one extra rk4Rhs, whose ks slot
+ *        0 is dead once the step is accumulated).
  *   csv  <nx> <p> <steps> <outprefix> [threads]
  *        Taylor-Green -> <steps> RK4 steps, then the reference's own
  *        snapshot writer (initXYZVFile + exportToXYZVFile, io.cpp:8-99)
@@ -79,6 +83,31 @@ static double tf_for_steps(int nx, int p, double L, int steps) {
   return tf;
 }
 
+/* Enstrophy of the state whose rk4Rhs just ran: the quadrature over the
+ * Gauss points of rho |curl v|^2 / 2, normalised like computeKE
+ * (solver.cpp:1007-1034) by rho0 (2 pi L)^3, from the reference's own
+ * interpolants uInterp3D = Interp3D u and DuInterp3D = Interp3D Dus
+ * (solver.cpp:495-514).  v = m/rho, d_j v_i = (d_j m_i - v_i d_j rho)/rho. */
+static double enstrophy(Solver& s, const darray& uI3, const darray& DuI3) {
+  darray xQ, wQ;
+  int nQ3D = gaussQuad3D(2 * s.order, xQ, wQ);
+  double J = s.mesh.minDX / 2.0 * s.mesh.minDY / 2.0 * s.mesh.minDZ / 2.0;
+  double total = 0.0;
+  for (int iK = 0; iK < s.mesh.nElements; ++iK) {
+    double el = 0.0;
+    for (int q = 0; q < nQ3D; ++q) {
+      double rho = uI3(q, 0, iK), v[3], G[3][3];
+      for (int i = 0; i < 3; ++i) v[i] = uI3(q, 1 + i, iK) / rho;
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) G[i][j] = (DuI3(q, 1 + i, iK, j) - DuI3(q, 0, iK, j) * v[i]) / rho;
+      double wx = G[2][1] - G[1][2], wy = G[0][2] - G[2][0], wz = G[1][0] - G[0][1];
+      el += J * wQ(q) * 0.5 * rho * (wx * wx + wy * wy + wz * wz);
+    }
+    total += el;
+  }
+  return total / (s.p.rho0 * std::pow(2 * M_PI * s.p.L, 3.0));
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: ldg_ref step|rhs ...\n");
@@ -101,6 +130,8 @@ int main(int argc, char** argv) {
     std::string out = argv[5];
     int dump_every = (!series && !csv && argc > 6) ? std::atoi(argv[6]) : steps;
     int threads = csv ? (argc > 6 ? std::atoi(argv[6]) : 1) : (argc > 7 ? std::atoi(argv[7]) : 1);
+    const int ens_every = (series && argc > 8) ? std::atoi(argv[8]) : 0;
+    std::vector<double> enst;
     scipy_openblas_set_num_threads(threads);
     MPIUtil mpi{};
     double size = M_PI * L;
@@ -170,6 +201,13 @@ int main(int argc, char** argv) {
           norms.push_back(acc);
         }
         for (long long j : idx) samples.push_back(s.u.data()[j]);
+        if (ens_every > 0 && (iStep + 1) % ens_every == 0) {
+          s.rk4UpdateCurr(uCurr, diagA, ks, 0);  // stage 0: uCurr = u
+          s.rk4Rhs(uCurr, uInterp2D, uInterp3D, Dus, DuInterp2D, DuInterp3D, toSend, toRecv, rk4Reqs,
+                   ks, 0);
+          enst.push_back(iStep + 1);
+          enst.push_back(enstrophy(s, uInterp3D, DuInterp3D));
+        }
         continue;
       }
       if (csv) continue;
@@ -189,6 +227,7 @@ int main(int argc, char** argv) {
     if (series) {
       write_doubles(out + ".norms", norms.data(), (long)norms.size());
       write_doubles(out + ".samples", samples.data(), (long)samples.size());
+      if (!enst.empty()) write_doubles(out + ".enst", enst.data(), (long)enst.size());
     }
     std::ofstream meta(out + ".meta");
     meta.precision(17);

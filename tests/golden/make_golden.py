@@ -5,8 +5,8 @@ oracle/build_ref.sh with the project's MPI/BLAS shim headers) and stores
 compact .npz fixtures.  Needs the reference checkout, so it runs only where
 that exists; the fixtures it writes are committed and travel everywhere.
 
-    python tests/golden/make_golden.py            # the small fixtures
-    python tests/golden/make_golden.py series     # the large-mesh series
+    REF_DIR=<reference checkout> python tests/golden/make_golden.py          # small fixtures
+    REF_DIR=<reference checkout> python tests/golden/make_golden.py series   # large-mesh series
 
 Fixtures (arrays use the reference layout u(node,var,elem) = numpy (nE,5,dofs)):
   tgv_n8_p2.npz     Taylor-Green 8^3 p=2, 100 RK4 steps: ke[100], dt,

@@ -91,3 +91,19 @@ def test_tf_for_steps_matches_reference_rule():
     import oracle
     for nx, p, steps in [(8, 2, 100), (32, 3, 200), (64, 4, 200), (16, 2, 7)]:
         assert ldg.tf_for_steps(nx, p, 1.0, steps) == oracle.tf_for_steps(nx, p, 1.0, steps)
+
+
+def test_noalloc_rejects_non_fp64_precision_before_device_work():
+    """ldg_rhs_noalloc computes in FP64 only: the mixed mode is refused as
+    unsupported and an unknown precision value as invalid, before any CUDA
+    call (so this runs without a device)."""
+    lib = ldg.load()
+    cfg = ldg.LdgConfig()
+    lib.ldg_config_default(ctypes.byref(cfg))
+    cfg.nx = cfg.ny = cfg.nz = 3
+    dummy = ctypes.c_void_p(16)  # never dereferenced: the checks come first
+    cfg.precision = 1  # LDG_MIXED_F32X2
+    assert lib.ldg_rhs_noalloc(ctypes.byref(cfg), dummy, dummy, None) == -5
+    assert b"FP64 only" in lib.ldg_last_error_message()
+    cfg.precision = 7
+    assert lib.ldg_rhs_noalloc(ctypes.byref(cfg), dummy, dummy, None) == -1
