@@ -214,6 +214,17 @@ int ldg_probe_fp64_peak(int device, double* tflops);
  * SM clock the probe ran at, in MHz (cycles over event time).  Either
  * pointer may be NULL.  (No reference counterpart.) */
 int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* sm_mhz);
+/* Measures the gradient pass's volume contraction alone (the product the
+ * reference evaluates as a dense DGEMM, solver.cpp:500, here the
+ * sum-factorised 1-D products along each direction) on the solver's
+ * current state, in one of four arithmetics: mode 0 FP64 FMAs, 1 FP32-pair
+ * FMAs, 2 FP32-pair compensated dot products, 3 tensor cores with exact
+ * integer slices (p = 4 only).  *ms: mean time of one launch over reps
+ * launches; *max_rel_err: largest difference from mode 0 over the first
+ * 2048 elements, relative to their largest value.  Overwrites the solver's
+ * scratch buffers (gradient, spare traces), not its state.  (No reference
+ * counterpart: it decides the arithmetic of the mixed path.) */
+int ldg_probe_contraction(ldg_solver* s, int mode, int reps, double* ms, double* max_rel_err);
 
 /* ---- Batched ensemble.  No reference counterpart (the reference runs one
  * problem per MPI job).  Members are independent problems, each an
@@ -227,8 +238,25 @@ int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* s
 typedef struct ldg_ensemble ldg_ensemble;
 int ldg_ensemble_create(const ldg_config* cfgs, int count, ldg_ensemble** out);
 int ldg_ensemble_destroy(ldg_ensemble* e);
-/* nsteps RK4 steps of every member (each with its own dt). */
+/* nsteps RK4 steps of every member (each with its own dt).  An RHS item
+ * waits (bounded) for its member's gradient items; a wait that runs out
+ * stops the step at a stage boundary with every member's step-start state
+ * intact.  By default the step is then re-run member by member with the
+ * solo kernels (the same bits) and the call carries on; with recovery off
+ * the call returns LDG_ERR_TIMEOUT and the state is that step's start.
+ * (The reference has no batched path; its MPI waits block, MPIUtil.cpp.) */
 int ldg_ensemble_step(ldg_ensemble* e, int nsteps);
+/* The bounded wait's limit in polls of ~100 ns (default 2^22, about half a
+ * second; 0 gives up as soon as a gradient item is still running) and
+ * whether a step that gave up is re-run member by member (recover != 0,
+ * the default) or reported as LDG_ERR_TIMEOUT. */
+int ldg_ensemble_set_wait_limit(ldg_ensemble* e, long long polls, int recover);
+/* Steps re-run member by member so far. */
+int ldg_ensemble_recovered_steps(const ldg_ensemble* e, long long* steps);
+/* Test hook, host-side fault injection: on != 0 raises member's
+ * gradient-item target by one, so that its RHS items wait for an item that
+ * never comes and their waits run out; on = 0 restores it. */
+int ldg_ensemble_inject_stall(ldg_ensemble* e, int member, int on);
 /* A member's state in the reference layout (host or device pointer). */
 int ldg_ensemble_get_state(ldg_ensemble* e, int member, double* u, int where);
 /* A member's computeKE series, one entry per step. */

@@ -15,6 +15,7 @@
 #include "../../include/ldg.h"
 #include "ldg_kernels.cuh"
 #include "ldg_ops.hpp"
+#include "ldg_tc.cuh"
 #include "ldg_problem.hpp"
 #include "ldg_closure.hpp"
 #include "ldg_io.hpp"
@@ -596,6 +597,37 @@ cudaError_t launch_traces_fp64(int N, const double* U, double* Tu, int nE, const
   cudaError_t e = d_attrs(N);
   if (e != cudaSuccess) return e;
   LDG_DISPATCH(N, (launch_traces<NN, double>(U, nullptr, Tu, nE, o, st)));
+}
+
+cudaError_t launch_grad_fp64(int N, const double* U, const double* Tu, double* Q, double* Tq, double* Fm,
+                             const DevOps& ops, const OpsT<double>& o, cudaStream_t st) {
+  cudaError_t e = d_attrs(N);
+  if (e != cudaSuccess) return e;
+  LDG_DISPATCH(N, (launch_grad<NN, double>(U, Tu, Q, Tq, Fm, nullptr, ops, o, st)));
+}
+
+cudaError_t launch_rhs_fp64(int N, const StageArgs<double>& a, const DevOps& ops, const OpsT<double>& o,
+                            cudaStream_t st) {
+  cudaError_t e = d_attrs(N);
+  if (e != cudaSuccess) return e;
+  StageCall c;
+  c.Us = a.Us;
+  c.Q = a.Q;
+  c.Tu = a.Tu;
+  c.Tq = a.Tq;
+  c.Fm = a.Fm;
+  c.Un = a.Un;
+  c.Uacc = a.Uacc;
+  c.Unext = a.Unext;
+  c.Tu_out = a.Tu_out;
+  c.Kout = a.Kout;
+  c.Kadd = a.Kadd;
+  c.diag = a.diag;
+  c.flag = a.flag;
+  c.cacc = a.cacc;
+  c.cnext = a.cnext;
+  c.stage = a.stage;
+  LDG_DISPATCH(N, (launch_rhs<NN, double>(c, ops, o, st)));
 }
 
 }  // namespace ldg
@@ -1198,6 +1230,86 @@ int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* s
 }
 
 int ldg_probe_fp64_peak(int device, double* tflops) { return ldg_probe_fp64(device, tflops, nullptr, nullptr); }
+
+}  // extern "C"
+
+namespace {
+template <int N>
+cudaError_t launch_contract(ldg_solver* s, int mode, const TcOps& tc) {
+  constexpr int EPC = Cfg<N>::EPC;
+  const int grid = (s->nE + EPC - 1) / EPC;
+  if (mode == 0) {
+    const size_t sm = sizeof(double) * EPC * kNS * Cfg<N>::n;
+    k_contract_point<N, double><<<grid, Cfg<N>::T, sm, s->stream>>>(s->Un, s->Q, s->nE, s->o64, 0);
+  } else if (mode <= 2) {
+    const size_t sm = sizeof(double) * EPC * kNS * Cfg<N>::n;
+    k_contract_point<N, dd><<<grid, Cfg<N>::T, sm, s->stream>>>((const float2*)s->Us, (float2*)s->Q, s->nE,
+                                                                 s->odd, mode == 2);
+  } else {
+    if constexpr (N == 5) {
+      static bool attr = false;
+      const size_t sm = sizeof(double) * 2 * (kNS + kNQ) * Cfg<N>::n;
+      if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_contract_tc<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+      }
+      k_contract_tc<5><<<(s->nE + 1) / 2, 256, sm, s->stream>>>((const float2*)s->Us, (float2*)s->Q, s->nE, tc);
+    } else {
+      return cudaErrorInvalidValue;
+    }
+  }
+  return cudaGetLastError();
+}
+cudaError_t d_contract(ldg_solver* s, int mode, const TcOps& tc) { LDG_DISPATCH(s->N, launch_contract<NN>(s, mode, tc)); }
+}  // namespace
+
+extern "C" {
+
+int ldg_probe_contraction(ldg_solver* s, int mode, int reps, double* ms, double* max_rel_err) {
+  if (!s || mode < 0 || mode > 3 || reps < 1) return fail(LDG_ERR_INVALID, "ldg_probe_contraction: bad arguments");
+  if (mode == 3 && s->N != 5) return fail(LDG_ERR_UNSUPPORTED, "ldg_probe_contraction: the tensor-core mode is built for p=4");
+  LDG_CUDA(cudaSetDevice(s->cfg.device));
+  LDG_CUDA(d_attrs(s->N));
+  const TcOps tc = make_tc_ops(s->ops, s->N);
+  // the FP32-pair copy of the state (what the mixed path's stage 0 reads),
+  // traces into the spare trace buffer; Q receives the contractions
+  LDG_CUDA(s_traces(s, true, s->Un, s->Us, s->Tu[1 - s->cur]));
+  const long long ne = std::min<long long>(s->nE, 2048);
+  const size_t cnt = (size_t)ne * kNQ * s->n;
+  std::vector<double> ref(cnt), got(cnt);
+  LDG_CUDA(d_contract(s, 0, tc));
+  LDG_CUDA(cudaMemcpyAsync(ref.data(), s->Q, cnt * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  LDG_CUDA(d_contract(s, mode, tc));  // warm-up, and the values compared
+  LDG_CUDA(cudaMemcpyAsync(got.data(), s->Q, cnt * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  cudaEvent_t e0, e1;
+  LDG_CUDA(cudaEventCreate(&e0));
+  LDG_CUDA(cudaEventCreate(&e1));
+  LDG_CUDA(cudaEventRecord(e0, s->stream));
+  for (int r = 0; r < reps; ++r) LDG_CUDA(d_contract(s, mode, tc));
+  LDG_CUDA(cudaEventRecord(e1, s->stream));
+  LDG_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  LDG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ms) *ms = t / reps;
+  double mx = 0.0, err = 0.0;
+  for (size_t i = 0; i < cnt; ++i) {
+    double v = got[i];
+    if (mode > 0) {  // FP32 pairs
+      float2 f;
+      std::memcpy(&f, &got[i], sizeof(f));
+      v = (double)f.x + (double)f.y;
+    }
+    mx = std::max(mx, std::fabs(ref[i]));
+    err = std::max(err, std::fabs(v - ref[i]));
+  }
+  if (max_rel_err) *max_rel_err = mx > 0 ? err / mx : err;
+  // the spare traces were overwritten with those of the pair copy of Un;
+  // a mixed solver's stage buffer now holds that same pair copy
+  return LDG_OK;
+}
 
 int ldg_save_checkpoint(ldg_solver* s, const char* path) {
   if (!s || !path || !*path) return fail(LDG_ERR_INVALID, "ldg_save_checkpoint: null solver or empty path");

@@ -8,8 +8,13 @@
 // spin) until all of i's gradient items are done.  Every gradient item was
 // dequeued before any RHS item and runs to completion without waiting, so a
 // wait depends only on CTAs that are already running: no grid-wide barrier
-// or co-residency is needed.  A wait that exceeds its iteration limit sets
-// an error flag and the CTA stops; the host reports LDG_ERR_TIMEOUT.
+// or co-residency is needed.  A wait that exceeds its iteration limit (a
+// runtime setting) sets the member's error flag and the CTA stops; the
+// stage launches after it in the same graph see the flag and return at
+// once, so the step stops at a stage boundary with the step's starting state
+// Un intact.  The host then either reports LDG_ERR_TIMEOUT or (the default)
+// recovers: it re-runs that step member by member with the solo kernels,
+// which give the same bits, and carries on with the graphs.
 //
 // Every item runs the per-element device code of the solo kernels
 // (grad_body / rhs_body), and the per-element arithmetic does not depend on
@@ -49,7 +54,7 @@ int fail(int code, const std::string& msg) {
 
 const double kRkB[4] = {1 / 6.0, 1 / 3.0, 1 / 3.0, 1 / 6.0};
 const double kRkA[3] = {0.5, 0.5, 1.0};
-constexpr long long kSpinLimit = 1LL << 22;  // x ~100 ns sleeps: gives up after ~0.5 s
+constexpr long long kDefaultWaitLimit = 1LL << 22;  // x ~100 ns sleeps: gives up after ~0.5 s
 
 // Device-resident description of one member (one per state parity).
 struct Member {
@@ -110,14 +115,16 @@ __device__ void run_item(const Member& m, const Item& it, int stage, int cur, in
   }
 }
 
+// err[0]: any wait gave up; err[1 + i]: a wait of member i gave up.
 template <int BD>
 __global__ void __launch_bounds__(BD) k_ensemble_stage(const Member* __restrict__ members,
                                                        const Item* __restrict__ items, int n_items, int* head,
                                                        int* done, const int* __restrict__ need, int stage, int cur,
-                                                       int* flag, int* err) {
+                                                       int* flag, int* err, long long wait_limit) {
   extern __shared__ double smem[];
   __shared__ int s_item;
   __shared__ int s_ok;
+  if (*(volatile int*)err) return;  // an earlier stage of this step gave up
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
     __syncthreads();
@@ -130,9 +137,10 @@ __global__ void __launch_bounds__(BD) k_ensemble_stage(const Member* __restrict_
         int ok = 1;
         long long spins = 0;
         while (atomicAdd(&done[it.inst], 0) < need[it.inst]) {
-          if (++spins > kSpinLimit) {
+          if (++spins > wait_limit) {
             ok = 0;
             atomicOr(err, 1);
+            atomicOr(err + 1 + it.inst, 1);
             break;
           }
           __nanosleep(100);
@@ -157,11 +165,11 @@ __global__ void __launch_bounds__(BD) k_ensemble_stage(const Member* __restrict_
 // Per-member KE after a step: the fixed-order compensated reduction of a
 // solo run (k_reduce in ldg_capi.cu), into ke[member * cap + step].
 __global__ void k_ensemble_ke(const Member* __restrict__ members, int count, const int* step, long long cap,
-                              double* ke) {
+                              double* ke, const int* err) {
   __shared__ double ss[1024];
   __shared__ double sc[1024];
   const int i = blockIdx.x;
-  if (i >= count) return;
+  if (i >= count || *(volatile const int*)err) return;
   const Member& m = members[i];
   double s = 0.0, c = 0.0;
   for (long j = threadIdx.x; j < m.ops.nE; j += blockDim.x) {
@@ -186,7 +194,9 @@ __global__ void k_ensemble_ke(const Member* __restrict__ members, int count, con
   if (threadIdx.x == 0) ke[(long long)i * cap + *step] = m.ops.ke_norm * (ss[0] + sc[0]);
 }
 
-__global__ void k_ensemble_advance(int* step) { *step += 1; }
+__global__ void k_ensemble_advance(int* step, const int* err) {
+  if (!*(volatile const int*)err) *step += 1;
+}
 
 size_t smem_bytes(int BD) {
   size_t mx = 0;
@@ -229,6 +239,10 @@ struct ldg_ensemble {
   size_t bytes = 0;
   float tune_ms[2][4] = {{0}};
   int tune_grid[4] = {0};
+  long long wait_limit = kDefaultWaitLimit;
+  int recover = 1;              // re-run a step that gave up, member by member
+  long long recovered = 0;      // steps re-run so far
+  std::vector<int> stalled;     // members whose gradient target is raised (test hook)
 };
 
 namespace {
@@ -261,11 +275,13 @@ int enqueue_stage(ldg_ensemble* e, int stage, int parity, int tile, int grid) {
   if (tile)
     k_ensemble_stage<256><<<grid, 256, smem_bytes(256), e->stream>>>(e->d_members[parity], e->d_items[1],
                                                                      e->n_items[1], e->d_head, e->d_done,
-                                                                     e->d_need[1], stage, 0, e->d_flag, e->d_err);
+                                                                     e->d_need[1], stage, 0, e->d_flag, e->d_err,
+                                                                     e->wait_limit);
   else
     k_ensemble_stage<128><<<grid, 128, smem_bytes(128), e->stream>>>(e->d_members[parity], e->d_items[0],
                                                                      e->n_items[0], e->d_head, e->d_done,
-                                                                     e->d_need[0], stage, 0, e->d_flag, e->d_err);
+                                                                     e->d_need[0], stage, 0, e->d_flag, e->d_err,
+                                                                     e->wait_limit);
   ENS_CUDA(cudaGetLastError());
   return LDG_OK;
 }
@@ -275,8 +291,9 @@ int enqueue_step(ldg_ensemble* e, int parity) {
   int st;
   for (int stage = 0; stage < 4; ++stage)
     if ((st = enqueue_stage(e, stage, parity, e->tile, e->grid))) return st;
-  k_ensemble_ke<<<e->count, 1024, 0, e->stream>>>(e->d_members[parity], e->count, e->d_step, e->ke_cap, e->d_ke);
-  k_ensemble_advance<<<1, 1, 0, e->stream>>>(e->d_step);
+  k_ensemble_ke<<<e->count, 1024, 0, e->stream>>>(e->d_members[parity], e->count, e->d_step, e->ke_cap, e->d_ke,
+                                                   e->d_err);
+  k_ensemble_advance<<<1, 1, 0, e->stream>>>(e->d_step, e->d_err);
   ENS_CUDA(cudaGetLastError());
   return LDG_OK;
 }
@@ -364,6 +381,75 @@ int check_flags(ldg_ensemble* e) {
   return LDG_OK;
 }
 
+// The host copy of member i for state parity p (Un and Uacc swapped for p=1).
+Member member_at(const ldg_ensemble* e, int i, int parity) {
+  Member m = e->members[i];
+  if (parity) std::swap(m.Un, m.Uacc);
+  return m;
+}
+
+// After a step that gave up: every member's step-start state Un is intact,
+// but the stages may have overwritten the traces of Un (the trace buffers
+// alternate per stage).  Rebuild them so that the step can start again.
+int restore_traces(ldg_ensemble* e, int parity) {
+  for (int i = 0; i < e->count; ++i) {
+    const Member m = member_at(e, i, parity);
+    ENS_CUDA(launch_traces_fp64(m.N, m.Un, m.Tu[0], m.ops.nE, m.o, e->stream));
+  }
+  return LDG_OK;
+}
+
+// Re-runs the step that starts at state parity `parity`, member by member,
+// with the solo kernels ldg_step launches (the same per-element arithmetic,
+// so the same bits as an uninterrupted ensemble step), then its KE and the
+// device step counter.  The error flags must be clear.
+int recover_step(ldg_ensemble* e, int parity) {
+  for (int i = 0; i < e->count; ++i) {
+    const Member m = member_at(e, i, parity);
+    for (int stage = 0; stage < 4; ++stage) {
+      const double* Uin = stage == 0 ? m.Un : m.Us;
+      double* Tu_in = m.Tu[(stage & 1) ? 1 : 0];
+      double* Tu_out = m.Tu[(stage & 1) ? 0 : 1];
+      ENS_CUDA(launch_grad_fp64(m.N, Uin, Tu_in, m.Q, m.Tq, m.Fm, m.ops, m.o, e->stream));
+      StageArgs<double> a{};
+      a.Us = Uin;
+      a.Q = m.Q;
+      a.Tu = Tu_in;
+      a.Tq = m.Tq;
+      a.Fm = m.Fm;
+      a.Un = m.Un;
+      a.Uacc = m.Uacc;
+      a.Unext = stage < 3 ? m.Us : nullptr;
+      a.Tu_out = Tu_out;
+      a.diag = stage == 3 ? m.diag : nullptr;
+      a.flag = e->d_flag;
+      a.cacc = m.cacc[stage];
+      a.cnext = stage < 3 ? m.cnext[stage] : 0.0;
+      a.stage = stage;
+      ENS_CUDA(launch_rhs_fp64(m.N, a, m.ops, m.o, e->stream));
+    }
+  }
+  k_ensemble_ke<<<e->count, 1024, 0, e->stream>>>(e->d_members[parity], e->count, e->d_step, e->ke_cap, e->d_ke,
+                                                   e->d_err);
+  k_ensemble_advance<<<1, 1, 0, e->stream>>>(e->d_step, e->d_err);
+  ENS_CUDA(cudaGetLastError());
+  return LDG_OK;
+}
+
+// Raises (on) or restores the gradient-item target of member i in both
+// tile shapes' need arrays.
+int set_need_offset(ldg_ensemble* e, int i, int delta) {
+  for (int tile = 0; tile < 2; ++tile) {
+    int v = 0;
+    ENS_CUDA(cudaMemcpyAsync(&v, e->d_need[tile] + i, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    ENS_CUDA(cudaStreamSynchronize(e->stream));
+    v += delta;
+    ENS_CUDA(cudaMemcpyAsync(e->d_need[tile] + i, &v, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+    ENS_CUDA(cudaStreamSynchronize(e->stream));
+  }
+  return LDG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -431,7 +517,7 @@ int ldg_ensemble_create(const ldg_config* cfgs, int count, ldg_ensemble** out) {
   }
   int* ints[5];
   for (int k = 0; k < 5; ++k) {
-    if ((st = ens_alloc(e, &p, sizeof(int) * (k == 1 ? count : 1)))) return bail(st);
+    if ((st = ens_alloc(e, &p, sizeof(int) * (k == 1 ? count : k == 3 ? count + 1 : 1)))) return bail(st);
     ints[k] = (int*)p;
   }
   e->d_head = ints[0];
@@ -439,7 +525,8 @@ int ldg_ensemble_create(const ldg_config* cfgs, int count, ldg_ensemble** out) {
   e->d_flag = ints[2];
   e->d_err = ints[3];
   e->d_step = ints[4];
-  if (cudaMemsetAsync(e->d_flag, 0, sizeof(int), e->stream) || cudaMemsetAsync(e->d_err, 0, sizeof(int), e->stream) ||
+  if (cudaMemsetAsync(e->d_flag, 0, sizeof(int), e->stream) ||
+      cudaMemsetAsync(e->d_err, 0, sizeof(int) * (count + 1), e->stream) ||
       cudaMemsetAsync(e->d_step, 0, sizeof(int), e->stream))
     return bail(fail(LDG_ERR_CUDA, "ensemble: counters"));
   // Work items per tile shape: every member's gradient items, then RHS items.
@@ -508,12 +595,67 @@ int ldg_ensemble_step(ldg_ensemble* e, int nsteps) {
   ENS_CUDA(cudaSetDevice(e->device));
   int st = ensure_ke(e, e->step + nsteps + 1);
   if (st) return st;
-  for (int it = 0; it < nsteps; ++it) {
-    ENS_CUDA(cudaGraphLaunch(e->exec[e->parity], e->stream));
-    e->parity ^= 1;  // u^{n+1} is in the other buffer
+  int left = nsteps;
+  while (left > 0) {
+    for (int it = 0; it < left; ++it) ENS_CUDA(cudaGraphLaunch(e->exec[(e->parity + it) & 1], e->stream));
+    int h[2] = {0, 0};  // error flag, device step counter
+    ENS_CUDA(cudaMemcpyAsync(&h[0], e->d_err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    ENS_CUDA(cudaMemcpyAsync(&h[1], e->d_step, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    ENS_CUDA(cudaStreamSynchronize(e->stream));
+    // steps completed: the graphs after a failed stage return at once and
+    // leave the device step counter where the failure happened
+    const int done = h[0] ? (int)(h[1] - e->step) : left;
+    e->parity ^= done & 1;  // u^{n+1} is in the other buffer
+    e->step += done;
+    left -= done;
+    if (!h[0]) break;
+    ENS_CUDA(cudaMemsetAsync(e->d_err, 0, sizeof(int) * (e->count + 1), e->stream));
+    if ((st = restore_traces(e, e->parity))) return st;
+    if (!e->recover) {
+      ENS_CUDA(cudaStreamSynchronize(e->stream));
+      return fail(LDG_ERR_TIMEOUT, "ensemble: a dependency wait exceeded its limit at step " +
+                                       std::to_string(e->step) + "; the state is that step's start");
+    }
+    if ((st = recover_step(e, e->parity))) return st;
+    e->parity ^= 1;
     e->step += 1;
+    e->recovered += 1;
+    left -= 1;
   }
   return check_flags(e);
+}
+
+int ldg_ensemble_set_wait_limit(ldg_ensemble* e, long long polls, int recover) {
+  if (!e || polls < 0) return fail(LDG_ERR_INVALID, "ensemble: bad arguments");
+  ENS_CUDA(cudaSetDevice(e->device));
+  ENS_CUDA(cudaStreamSynchronize(e->stream));
+  e->recover = recover ? 1 : 0;
+  if (polls == e->wait_limit) return LDG_OK;
+  e->wait_limit = polls;
+  return capture_graphs(e);  // the limit is a launch argument the graphs bake in
+}
+
+int ldg_ensemble_recovered_steps(const ldg_ensemble* e, long long* steps) {
+  if (!e || !steps) return fail(LDG_ERR_INVALID, "ensemble: bad arguments");
+  *steps = e->recovered;
+  return LDG_OK;
+}
+
+int ldg_ensemble_inject_stall(ldg_ensemble* e, int member, int on) {
+  if (!e || member < 0 || member >= e->count) return fail(LDG_ERR_INVALID, "ensemble: bad arguments");
+  ENS_CUDA(cudaSetDevice(e->device));
+  ENS_CUDA(cudaStreamSynchronize(e->stream));
+  auto it = std::find(e->stalled.begin(), e->stalled.end(), member);
+  const bool is_on = it != e->stalled.end();
+  if (on && !is_on) {
+    e->stalled.push_back(member);
+    return set_need_offset(e, member, +1);
+  }
+  if (!on && is_on) {
+    e->stalled.erase(it);
+    return set_need_offset(e, member, -1);
+  }
+  return LDG_OK;
 }
 
 int ldg_ensemble_get_state(ldg_ensemble* e, int member, double* u, int where) {

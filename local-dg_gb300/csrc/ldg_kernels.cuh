@@ -127,10 +127,10 @@ __device__ __forceinline__ void write_traces(const T* sU, int ne, long e0, typen
     const T* lvec = (f & 1) ? o.lp : o.lm;
     const int st = stride_of<N>(l);
     const T* row = sU + (es * kNS + v) * n + face_point<N>(l, 0, t);
-    T acc{};
+    Acc<T> acc;
 #pragma unroll
-    for (int qn = 0; qn < N; ++qn) acc = fma(lvec[qn], row[qn * st], acc);
-    Real<T>::st(Tu + (e0 + es) * 6 * kNS * nf + r, acc);
+    for (int qn = 0; qn < N; ++qn) acc.add(lvec[qn], row[qn * st]);
+    Real<T>::st(Tu + (e0 + es) * 6 * kNS * nf + r, acc.get());
   }
 }
 
@@ -238,12 +238,22 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
         const T* line = sU + (es * kNS + v) * n + b;
-        T acc{};
-#pragma unroll
-        for (int r = 0; r < N; ++r) acc = fma(row[r], line[r * st], acc);
         const T tp = sTp[((es * 3 + l) * kNS + v) * nf + t];
         const T tm = sTm[((es * 3 + l) * kNS + v) * nf + t];
-        const T g = lp * tp - lm * tm - acc;
+        T g;
+        if constexpr (std::is_same<T, double>::value) {
+          T acc{};
+#pragma unroll
+          for (int r = 0; r < N; ++r) acc = fma(row[r], line[r * st], acc);
+          g = lp * tp - lm * tm - acc;
+        } else {  // one compensated 7-term dot product
+          Acc<T> acc;
+#pragma unroll
+          for (int r = 0; r < N; ++r) acc.add(-row[r], line[r * st]);
+          acc.add(lp, tp);
+          acc.add(-lm, tm);
+          g = acc.get();
+        }
         grad[l * kNS + v] = g;
         sQ[(es * kNQ + l * kNS + v) * n + q] = g;
         R::st(Q + ((e0 + es) * kNQ + l * kNS + v) * n + q, g);
@@ -283,10 +293,10 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
     int cc = r2 / nf, t = r2 - cc * nf;
     const int st = stride_of<N>(l);
     const T* row = sQ + (es2 * kNQ + cc) * n + face_point<N>(l, 0, t);
-    T acc{};
+    Acc<T> acc;
 #pragma unroll
-    for (int qn = 0; qn < N; ++qn) acc = fma(o.lm[qn], row[qn * st], acc);
-    R::st(Tq + (e0 + es2) * 3 * kNQ * nf + r, acc);
+    for (int qn = 0; qn < N; ++qn) acc.add(o.lm[qn], row[qn * st]);
+    R::st(Tq + (e0 + es2) * 3 * kNQ * nf + r, acc.get());
   }
 }
 
@@ -337,13 +347,13 @@ __device__ __forceinline__ void ke_tail(const T* sU, T* scr, int ne, long e0, do
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const T* row = sin + (es * instride + v) * n + b;
-        T acc{};
+        Acc<T> acc;
 #pragma unroll
         for (int r = 0; r < N; ++r) {
-          if constexpr (std::is_same<T, double>::value) acc = fma(ops.Bi[c[l] * N + r], row[r * st], acc);
-          else acc = fma(o.Bi[c[l] * N + r], row[r * st], acc);
+          if constexpr (std::is_same<T, double>::value) acc.add(ops.Bi[c[l] * N + r], row[r * st]);
+          else acc.add(o.Bi[c[l] * N + r], row[r * st]);
         }
-        sout[(es * 4 + v) * n + q] = acc;
+        sout[(es * 4 + v) * n + q] = acc.get();
       }
     }
     __syncthreads();
@@ -509,12 +519,12 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
 #pragma unroll
       for (int v = 0; v < kNS; ++v) {
         const T* line = sF + (es * kNQ + l * kNS + v) * n + b;
-        T acc = K[v];
+        Acc<T> acc(K[v]);
 #pragma unroll
-        for (int r = 0; r < N; ++r) acc = fma(row[r], line[r * st], acc);
-        acc = fma(lm, sFs[((es * 6 + 2 * l) * kNS + v) * nf + t], acc);
-        acc = fma(lp, sFs[((es * 6 + 2 * l + 1) * kNS + v) * nf + t], acc);
-        K[v] = acc;
+        for (int r = 0; r < N; ++r) acc.add(row[r], line[r * st]);
+        acc.add(lm, sFs[((es * 6 + 2 * l) * kNS + v) * nf + t]);
+        acc.add(lp, sFs[((es * 6 + 2 * l + 1) * kNS + v) * nf + t]);
+        K[v] = acc.get();
       }
     }
   }

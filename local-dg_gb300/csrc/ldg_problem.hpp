@@ -6,7 +6,7 @@
 #include <string>
 
 #include "../../include/ldg.h"
-#include "ldg_device.cuh"
+#include "ldg_kernels.cuh"
 #include "ldg_ops.hpp"
 
 namespace ldg {
@@ -39,6 +39,13 @@ cudaError_t launch_transform_any(int N, const double* in, double* out, int nE, c
 // FP64 face traces of an FP64 state.
 cudaError_t launch_traces_fp64(int N, const double* U, double* Tu, int nE, const OpsT<double>& o,
                                cudaStream_t st);
+
+// One gradient pass and one RHS/RK pass of the solo FP64 kernels (the
+// launches ldg_step makes), for callers outside the solver handle.
+cudaError_t launch_grad_fp64(int N, const double* U, const double* Tu, double* Q, double* Tq, double* Fm,
+                             const DevOps& ops, const OpsT<double>& o, cudaStream_t st);
+cudaError_t launch_rhs_fp64(int N, const StageArgs<double>& a, const DevOps& ops, const OpsT<double>& o,
+                            cudaStream_t st);
 
 void set_last_error(const std::string& msg);
 

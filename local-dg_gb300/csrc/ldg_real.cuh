@@ -95,6 +95,43 @@ __device__ __forceinline__ dd fabs(dd x) { return x.h < 0.0f ? -x : x; }
 // Scaling by a power of two is exact.
 __device__ __forceinline__ dd scale2(dd x, float p2) { return {x.h * p2, x.l * p2}; }
 
+// Dot-product accumulators: sum_k a_k b_k + c term by term.
+// Acc<double> is the FMA chain of the FP64 path (bit for bit the loops it
+// replaces).  Acc<dd> follows the "Dot2" scheme of Ogita, Rump and Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005: the
+// high parts' products are split exactly (TwoProd with FMA) and summed with
+// TwoSum, and every error term and low-part product goes into one FP32
+// accumulator; the pair is renormalised once at the end.  About 12 FP32
+// operations per term against 15 for a renormalising pair FMA, with shorter
+// dependency chains; the result is as accurate as if computed in twice the
+// working precision (error ~ K u^2 sum |a_k b_k|, u = 2^-24).
+template <class T>
+struct Acc;
+
+template <>
+struct Acc<double> {
+  double v;
+  __device__ __forceinline__ explicit Acc(double c = 0.0) : v(c) {}
+  __device__ __forceinline__ void add(double a, double b) { v = ::fma(a, b, v); }
+  __device__ __forceinline__ double get() const { return v; }
+};
+
+template <>
+struct Acc<dd> {
+  float s, c;
+  __device__ __forceinline__ explicit Acc(dd x = dd{0.0f, 0.0f}) : s(x.h), c(x.l) {}
+  __device__ __forceinline__ void add(dd a, dd b) {
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = __fmaf_rn(a.h, b.h, -p);
+    const dd t = dd_two_sum(s, p);
+    s = t.h;
+    c = __fmaf_rn(a.h, b.l, c);
+    c = __fmaf_rn(a.l, b.h, c);
+    c = __fadd_rn(c, __fadd_rn(t.l, e));
+  }
+  __device__ __forceinline__ dd get() const { return dd_two_sum(s, c); }
+};
+
 // ----------------------------------------------------------------- traits
 template <class T>
 struct Real;

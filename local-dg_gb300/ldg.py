@@ -145,6 +145,7 @@ SIGNATURES = {
     "ldg_kernel_times": (_i, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _i, _i]),
     "ldg_probe_fp64_peak": (_i, [_i, _dp]),
     "ldg_probe_fp64": (_i, [_i, _dp, _dp, _dp]),
+    "ldg_probe_contraction": (_i, [_vp, _i, _i, _dp, _dp]),
     "ldg_rhs_noalloc": (_i, [ctypes.POINTER(LdgConfig), _vp, _vp, _vp]),
     "ldg_ensemble_create": (_i, [ctypes.POINTER(LdgConfig), _i, ctypes.POINTER(_vp)]),
     "ldg_ensemble_destroy": (_i, [_vp]),
@@ -154,6 +155,9 @@ SIGNATURES = {
     "ldg_ensemble_member_info": (_i, [_vp, _i, ctypes.POINTER(LdgInfo)]),
     "ldg_ensemble_tuning": (_i, [_vp, _ip, _ip, ctypes.POINTER(ctypes.c_float), _i]),
     "ldg_ensemble_stream": (_vp, [_vp]),
+    "ldg_ensemble_set_wait_limit": (_i, [_vp, ctypes.c_longlong, _i]),
+    "ldg_ensemble_recovered_steps": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "ldg_ensemble_inject_stall": (_i, [_vp, _i, _i]),
     "ldg_closure_create": (_i, [_i, _i, ctypes.c_ulonglong, _i, ctypes.POINTER(_vp)]),
     "ldg_closure_destroy": (_i, [_vp]),
     "ldg_closure_add_samples": (_i, [_vp, _vp, _vp]),
@@ -363,6 +367,17 @@ class Solver:
 
     def dg_time_step(self) -> None:
         _check(load().ldg_time_step(self._h), "ldg_time_step")
+
+    CONTRACTION_MODES = {"fp64": 0, "pair_fma": 1, "pair_dot2": 2, "tensor_core_slices": 3}
+
+    def probe_contraction(self, mode: str, reps: int = 10):
+        """Times the gradient pass's volume contraction in one arithmetic
+        (see CONTRACTION_MODES) on the current state: (ms per launch, largest
+        difference from FP64 relative to the largest value)."""
+        ms, err = ctypes.c_double(), ctypes.c_double()
+        _check(load().ldg_probe_contraction(self._h, self.CONTRACTION_MODES[mode], reps, ctypes.byref(ms),
+                                            ctypes.byref(err)), "ldg_probe_contraction")
+        return ms.value, err.value
 
     def diagnostics(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
@@ -651,3 +666,19 @@ class Ensemble:
     @property
     def stream(self) -> int:
         return load().ldg_ensemble_stream(self._h)
+
+    def set_wait_limit(self, polls: int, recover: bool = True) -> None:
+        """Bounded-wait limit (polls of ~100 ns) and whether a step whose wait
+        ran out is re-run member by member (True) or reported (False)."""
+        _check(load().ldg_ensemble_set_wait_limit(self._h, polls, 1 if recover else 0),
+               "ldg_ensemble_set_wait_limit")
+
+    def recovered_steps(self) -> int:
+        n = ctypes.c_longlong()
+        _check(load().ldg_ensemble_recovered_steps(self._h, ctypes.byref(n)), "ldg_ensemble_recovered_steps")
+        return n.value
+
+    def inject_stall(self, member: int, on: bool = True) -> None:
+        """Test hook: member's RHS items wait for a gradient item that never
+        comes (host-side fault injection)."""
+        _check(load().ldg_ensemble_inject_stall(self._h, member, 1 if on else 0), "ldg_ensemble_inject_stall")

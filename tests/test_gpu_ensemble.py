@@ -102,3 +102,83 @@ def test_ensemble_reports_nonfinite():
         with pytest.raises(ldg.LdgError) as ei:
             ens.step(1)
         assert ei.value.status == -4
+
+
+def solo_run(c, steps):
+    with ldg.Solver(c.p, c.nx, tf=c.tf, Re=c.Re, perturb_amp=c.perturb_amp, seed=c.seed,
+                    instance=c.instance) as s:
+        s.step(steps)
+        return s.get_state(), s.ke_history()
+
+
+@pytest.mark.gpu
+def test_ensemble_wait_timeout_is_reported_and_state_kept():
+    """A member whose RHS items wait for a gradient item that never comes
+    (host-injected): with recovery off, the step returns LDG_ERR_TIMEOUT
+    after the short wait limit, the state stays at the step's start, and
+    the ensemble steps on normally once the stall is lifted."""
+    cfgs = small_configs(4)[:4]
+    with ldg.Ensemble(cfgs) as ens:
+        ens.step(1)
+        before = [ens.get_state(i) for i in range(4)]
+        ens.set_wait_limit(1 << 14, recover=False)
+        ens.inject_stall(2)
+        with pytest.raises(ldg.LdgError) as ei:
+            ens.step(2)
+        assert ei.value.status == -7  # LDG_ERR_TIMEOUT
+        assert ens.info(0).step == 1 and len(ens.ke_history(0)) == 1
+        for i in range(4):
+            assert np.array_equal(ens.get_state(i), before[i])
+        ens.inject_stall(2, on=False)
+        ens.set_wait_limit(1 << 22, recover=True)
+        ens.step(3)
+        assert ens.recovered_steps() == 0
+        after = [ens.get_state(i) for i in range(4)]
+    for i, c in enumerate(cfgs):
+        u, ke = solo_run(c, 4)
+        assert np.array_equal(after[i], u), f"member {i} differs from its solo run"
+
+
+@pytest.mark.gpu
+def test_ensemble_recovers_a_stalled_step_member_by_member():
+    """With recovery on (the default), each step whose wait runs out is
+    re-run member by member with the solo kernels: every member, the
+    stalled one included, still equals its solo run bit for bit."""
+    steps = 3
+    cfgs = small_configs(steps)
+    with ldg.Ensemble(cfgs) as ens:
+        ens.set_wait_limit(1 << 14, recover=True)
+        ens.inject_stall(4)
+        ens.step(2)
+        assert ens.recovered_steps() == 2
+        ens.inject_stall(4, on=False)
+        ens.set_wait_limit(1 << 22, recover=True)
+        ens.step(1)
+        assert ens.recovered_steps() == 2
+        states = [ens.get_state(i) for i in range(len(cfgs))]
+        kes = [ens.ke_history(i) for i in range(len(cfgs))]
+    for i, c in enumerate(cfgs):
+        u, ke = solo_run(c, steps)
+        assert np.array_equal(states[i], u), f"member {i} differs from its solo run"
+        assert np.array_equal(kes[i], ke), f"member {i} KE differs from its solo run"
+
+
+@pytest.mark.gpu
+def test_full_ensemble_members_equal_solo_runs_bitwise():
+    """The 64-member batched configuration (element counts from
+    {8^3,12^3,16^3,24^3}, p from {2,3,4}, Re log-uniform in [400,3200],
+    seeded perturbations): after 2 steps, one member of each order equals
+    its solo run bit for bit."""
+    steps = 2
+    cfgs = ldg.ensemble_configs(64, seed=2024, steps=1000)
+    pick = {}
+    for i, c in enumerate(cfgs):
+        pick.setdefault(c.p, i)
+    with ldg.Ensemble(cfgs) as ens:
+        ens.step(steps)
+        got = {i: (ens.get_state(i), ens.ke_history(i)) for i in pick.values()}
+    assert sorted(pick) == [2, 3, 4]
+    for i, (u_e, ke_e) in got.items():
+        u, ke = solo_run(cfgs[i], steps)
+        assert np.array_equal(u_e, u), f"member {i} (p={cfgs[i].p}) differs from its solo run"
+        assert np.array_equal(ke_e, ke)

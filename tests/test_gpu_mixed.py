@@ -98,3 +98,17 @@ def test_mixed_nonfinite_reported():
         with pytest.raises(ldg.LdgError) as ei:
             s.step(1)
         assert ei.value.status == -4
+
+
+@pytest.mark.parametrize("mode,tol", [("pair_fma", 1e-13), ("pair_dot2", 1e-13), ("tensor_core_slices", 1e-8)])
+def test_contraction_arithmetics_against_fp64(mode, tol):
+    """The gradient pass's volume contraction in the mixed path's candidate
+    arithmetics, against FP64 on a perturbed Taylor-Green state at 6^3 p=4:
+    the FP32 pairs keep ~2^-44; the tensor-core scheme with three exact
+    10-bit slices per operand and levels 2..4 keeps ~2^-30."""
+    with ldg.Solver(4, 6, perturb_amp=1e-2, seed=5) as s:
+        ms, err = s.probe_contraction(mode, reps=2)
+    assert ms > 0
+    assert err <= tol, (mode, err)
+    if mode == "tensor_core_slices":
+        assert err > 1e-13  # it is the sliced arithmetic that ran, not FP64
