@@ -334,6 +334,28 @@ def ensemble_variant(count, K, W, dev):
     return out
 
 
+def contraction_probe(s, reps=5):
+    """The gradient pass's volume contraction alone (15 sum-factorised 1-D
+    products per Gauss point) on the solver's state, in the four candidate
+    arithmetics: ms per launch and the largest difference from FP64."""
+    out = {}
+    for mode in ("fp64", "pair_fma", "pair_dot2", "tensor_core_slices"):
+        ms, err = s.probe_contraction(mode, reps=reps)
+        out[mode] = {"ms": ms, "max_rel_err_vs_fp64": err}
+    return out
+
+
+def run_contraction_probe(args):
+    import torch
+    import ldg
+    torch.cuda.set_device(0)
+    ldg.load()
+    with ldg.Solver(args.p, args.nx, device=0, perturb_amp=1e-2, seed=5) as s:
+        print(json.dumps({"workload": f"tgv_{args.nx}^3_p{args.p}", "contraction_probe":
+                          contraction_probe(s, reps=args.probe_reps)}))
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -413,6 +435,9 @@ def run_ours(args):
                                     "flops_per_dof": ncu["fp64_flops"] / N ** 3,
                                     "flops_source": "ncu instruction counts, 24^3 p=4 capture"}
     kernel_ms = {k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1)} for k, v in kt.items()}
+    contraction = None
+    if args.precision == "fp64" and not args.no_variants and args.p == 4:
+        contraction = contraction_probe(s, reps=5)
     s.close()
 
     # ---- the mixed-precision variant on the same workload, and its error
@@ -429,6 +454,8 @@ def run_ours(args):
             mixed["accuracy_vs_fp64"] = accuracy_vs_fp64(args.p, args.nx, args.accuracy_steps, dev)
         variants["mixed_f32x2"] = mixed
 
+    if contraction:
+        variants["contraction_probe"] = contraction
     if args.precision == "fp64" and not args.no_variants and args.ensemble > 0:
         variants["ensemble"] = ensemble_variant(args.ensemble, K, W, dev)
 
@@ -469,7 +496,12 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--ensemble", type=int, default=64, help="members of the ensemble variant (0: skip)")
+    ap.add_argument("--contraction-probe", action="store_true",
+                    help="only time the gradient volume contraction in each arithmetic")
+    ap.add_argument("--probe-reps", type=int, default=5)
     args = ap.parse_args()
+    if args.contraction_probe:
+        return run_contraction_probe(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

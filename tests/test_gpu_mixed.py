@@ -100,12 +100,15 @@ def test_mixed_nonfinite_reported():
         assert ei.value.status == -4
 
 
-@pytest.mark.parametrize("mode,tol", [("pair_fma", 1e-13), ("pair_dot2", 1e-13), ("tensor_core_slices", 1e-8)])
+@pytest.mark.parametrize("mode,tol", [("pair_fma", 1e-13), ("pair_dot2", 1e-13), ("tensor_core_slices", 1e-7)])
 def test_contraction_arithmetics_against_fp64(mode, tol):
     """The gradient pass's volume contraction in the mixed path's candidate
-    arithmetics, against FP64 on a perturbed Taylor-Green state at 6^3 p=4:
-    the FP32 pairs keep ~2^-44; the tensor-core scheme with three exact
-    10-bit slices per operand and levels 2..4 keeps ~2^-30."""
+    arithmetics, against FP64 on a perturbed Taylor-Green state at 6^3 p=4,
+    relative to the largest output: the FP32 pairs keep ~2^-44; the
+    tensor-core scheme (three exact 10-bit slices per operand, levels 2..4)
+    keeps ~2^-30 of max|A| max|x| per line, which the energy lines (E ~ 178,
+    and the weak derivative's rows do not sum to zero) make ~1e-8 of the
+    largest output."""
     with ldg.Solver(4, 6, perturb_amp=1e-2, seed=5) as s:
         ms, err = s.probe_contraction(mode, reps=2)
     assert ms > 0

@@ -1,14 +1,17 @@
 """GPU parity at the benchmark meshes, and the enstrophy diagnostic.
 
-Taylor-Green 32^3 p=3 for 200 RK4 steps and 64^3 p=4 for 2 steps against
-the reference's own run (tests/golden/series_*.npz, made by
-tests/golden/make_golden.py series): after every step the KE series, the
-per-variable sums of squares and a seeded sample of state entries.  Bar:
-relative L2 <= 1e-12 per step on the sample (and relative 1e-12 on the KE
-and on the norms).  The reference computes no enstrophy; the GPU's
-enstrophy functional is pinned against a numpy evaluation on the
-reference's own LDG gradient (Dus) of the golden RHS fixtures, and its time
-series along the 32^3 run is recorded and checked to be smooth.
+Taylor-Green 32^3 p=3 for 200 RK4 steps against the reference's own run,
+and 64^3 p=4 for 200 RK4 steps against the oracle's factored chain, whose
+first 20 steps are themselves checked against the reference's own run
+(tests/golden/series_*.npz, made by tests/golden/make_golden.py series):
+after every step the KE series, the per-variable sums of squares and a
+seeded sample of state entries.  Bar: relative L2 <= 1e-12 per step on the
+sample (and relative 1e-12 on the KE and on the norms).  The reference
+computes no enstrophy; the GPU's enstrophy functional is pinned against a
+numpy evaluation on the reference's own LDG gradient (Dus) of the golden
+RHS fixtures, against the reference's gradient along the first 20 steps at
+64^3 p=4 and the oracle's along all 200, and its time series along the
+32^3 run is recorded and checked to be smooth.
 """
 import os
 
@@ -30,7 +33,7 @@ def load(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["series_n32_p3.npz", "series_n64_p4.npz"])
+@pytest.mark.parametrize("name", ["series_n32_p3.npz"])
 def test_benchmark_mesh_per_step_parity(name):
     z = load(name)
     stem = name.split(".")[0]  # series_n<nx>_p<p>
@@ -66,6 +69,47 @@ def test_benchmark_mesh_per_step_parity(name):
         enst = np.asarray(enst)
         assert np.all(np.isfinite(enst)) and enst[-1] > enst[0]
         assert abs(enst[0] - 0.375) < 0.01
+
+
+@pytest.mark.gpu
+def test_64_cubed_p4_200_steps_per_step_parity():
+    """The headline configuration: Taylor-Green 64^3 hexes, p=4, Re=1600,
+    200 RK4 steps at the reference's dt.  Every step: KE, per-variable
+    norms and 1024 sampled entries against the oracle's 200-step series;
+    steps 1..20 also against the reference's own run (4096 sampled
+    entries); enstrophy against the reference's gradient (steps 4..20) and
+    the oracle's (every 10 steps)."""
+    z = load("series_n64_p4.npz")
+    if "ref_steps" not in z.files:
+        pytest.skip("series_n64_p4.npz is the 2-step reference-only fixture")
+    steps, ref_steps = int(z["steps"]), int(z["ref_steps"])
+    assert steps == 200 and ref_steps >= 20
+    ens_ref = dict(zip(z["ref_enst_steps"].tolist(), z["ref_enst"].tolist()))
+    ens_or = dict(zip(z["enst_steps"].tolist(), z["enst"].tolist()))
+    with ldg.Solver(4, 64, steps=steps) as s:
+        assert s.timesteps == steps
+        assert abs(s.dt - float(z["dt"])) <= 1e-15 * float(z["dt"])
+        u = np.empty(s.shape)
+        for k in range(1, steps + 1):
+            s.step(1)
+            s.get_state(u)
+            flat = u.ravel()
+            assert rel_l2(flat[z["idx"]], z["samples"][k - 1]) <= TOL, k
+            norms = np.sqrt(np.einsum("evq,evq->v", u, u))
+            tot = np.sqrt(np.sum(z["norms"][k - 1]))
+            assert np.max(np.abs(norms - np.sqrt(z["norms"][k - 1]))) <= TOL * tot, k
+            if k <= ref_steps:
+                assert rel_l2(flat[z["ref_idx"]], z["ref_samples"][k - 1]) <= TOL, k
+                assert np.max(np.abs(norms - np.sqrt(z["ref_norms"][k - 1]))) <= \
+                    TOL * np.sqrt(np.sum(z["ref_norms"][k - 1])), k
+            if k in ens_ref or k in ens_or:
+                ens = s.diagnostics()[2]
+                for table in (ens_ref, ens_or):
+                    if k in table:
+                        assert abs(ens - table[k]) <= TOL * abs(table[k]), (k, ens, table[k])
+        ke = s.ke_history()
+    assert np.max(np.abs(ke - z["ke"]) / np.abs(z["ke"])) <= TOL
+    assert np.max(np.abs(ke[:ref_steps] - z["ref_ke"]) / np.abs(z["ref_ke"])) <= TOL
 
 
 def enstrophy_numpy(u_nodal, q_nodal, nx, p, L=1.0):

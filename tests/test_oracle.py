@@ -143,3 +143,38 @@ def test_oracle_matches_reference_series_at_32_cubed_p3():
         assert rel_l2(u.ravel()[z["idx"]], z["samples"][k]) <= 1e-12
         norms = np.sqrt(np.einsum("evq,evq->v", u, u))
         assert np.max(np.abs(norms - np.sqrt(z["norms"][k]))) <= 1e-12 * np.sqrt(np.sum(z["norms"][k]))
+
+
+@pytest.mark.parametrize("name", ["rhs_n3_p1", "rhs_n3_p2", "rhs_n4_p3", "rhs_n3_p4", "rhs_n4_p2"])
+def test_factored_rhs_matches_reference(name):
+    """The Kronecker-factored operator chain (the oracle's mode for long
+    runs at the benchmark meshes) against the reference's RHS."""
+    z = load(name + ".npz")
+    nx, p = int(name.split("_")[1][1:]), int(name.split("_")[2][1:])
+    o = oracle.Oracle(nx, p)
+    o.set_factored(True)
+    assert rel_l2(o.rhs(z["u0"]), z["k"]) <= TOL
+
+
+def test_factored_oracle_matches_reference_series_at_32_cubed_p3():
+    """The first three steps of the reference's 32^3 p=3 run with the
+    factored chain (all 200 steps agree to <= 1.3e-14 on the samples; the
+    generator of the 64^3 p=4 fixture checks its own 20-step window)."""
+    z = np.load(os.path.join(GOLDEN, "series_n32_p3.npz"))
+    o = oracle.Oracle(32, 3, steps=int(z["steps"]), threads=os.cpu_count() or 1)
+    o.set_factored(True)
+    u = o.initial_condition()
+    for k in range(3):
+        u, ke = o.step(u, 1)
+        assert abs(ke[0] - z["ke"][k]) <= 1e-12 * z["ke"][k]
+        assert rel_l2(u.ravel()[z["idx"]], z["samples"][k]) <= 1e-12
+
+
+def test_factored_enstrophy_equals_dense():
+    """Enstrophy from the factored gradient equals the dense chain's."""
+    z = load("rhs_n4_p3.npz")
+    a = oracle.Oracle(4, 3)
+    b = oracle.Oracle(4, 3)
+    b.set_factored(True)
+    ea, eb = a.enstrophy(z["u0"]), b.enstrophy(z["u0"])
+    assert abs(ea - eb) <= 1e-12 * abs(ea)
