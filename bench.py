@@ -334,6 +334,54 @@ def ensemble_variant(count, K, W, dev):
     return out
 
 
+CLOSURE_RECORD = os.path.join(ROOT, "local-dg_gb300", "examples", "closure_c5_result.json")
+
+
+def learned_variant(K, W, dev):
+    """The learned-closure configuration: a coarse 16^3 p=2 FP64 Taylor-Green
+    solver timed without and with the closure attached (per-element MLP
+    inference, energy projection and fallback in every RK stage).  The
+    network is trained briefly here on samples from a 32^3 p=4 state, which
+    is enough to time its inference; the accuracy of a fully trained closure
+    comes from the committed record of the closure study
+    (closure_c5_result.json, made by examples/closure_tgv.py)."""
+    import torch
+    import ldg
+    out = {"coarse": "16^3 p=2 FP64, CFL 0.01", "network": "540-128-128-135 GELU, BF16 mma.sync"}
+    with ldg.Closure(p=2, hidden=128, seed=7, device=dev) as c, \
+            ldg.Solver(4, 32, steps=10, perturb_amp=1e-2, seed=1001, device=dev) as fine, \
+            ldg.Solver(2, 16, steps=10, device=dev) as ws:
+        c.add_samples(fine, ws)
+        c.finalize(0, c.samples)
+        c.train(0, c.samples, iters=200, batch=1024)
+        rates = {}
+        for name, attach in (("plain", False), ("closure", True)):
+            with ldg.Solver(2, 16, steps=max(K + W, 1) + 8, perturb_amp=1e-2, seed=2002, device=dev) as s:
+                if attach:
+                    s.attach_closure(c)
+                stream = torch.cuda.ExternalStream(s.stream, device=dev)
+                s.step(W)
+                s.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                s.step(K)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                rates[name] = {"value": s.dofs * s.nE * 4 * K / (ms * 1e-3), "ms_per_step": ms / K}
+        out.update(rates)
+        out["closure_overhead"] = rates["closure"]["ms_per_step"] / rates["plain"]["ms_per_step"]
+    try:
+        with open(CLOSURE_RECORD) as f:
+            rec = json.load(f)
+        out["recorded_a_posteriori"] = {"source": os.path.relpath(CLOSURE_RECORD, ROOT),
+                                        "config": rec.get("config"), "a_posteriori": rec.get("a_posteriori")}
+    except OSError:
+        out["recorded_a_posteriori"] = None
+    return out
+
+
 def contraction_probe(s, reps=5):
     """The gradient pass's volume contraction alone (15 sum-factorised 1-D
     products per Gauss point) on the solver's state, in the four candidate
@@ -458,6 +506,8 @@ def run_ours(args):
         variants["contraction_probe"] = contraction
     if args.precision == "fp64" and not args.no_variants and args.ensemble > 0:
         variants["ensemble"] = ensemble_variant(args.ensemble, K, W, dev)
+    if args.precision == "fp64" and not args.no_variants:
+        variants["learned"] = learned_variant(K, W, dev)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,

@@ -285,6 +285,15 @@ int ldg_closure_destroy(ldg_closure* c);
  * mesh must refine the coarse one uniformly, same domain), the coarse
  * gradient and RHS of the projected state.  Both solvers FP64. */
 int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse);
+/* Solver in the loop.  ldg_closure_project_state makes the L2 projection of
+ * the fine solver's state the coarse solver's state (no samples).
+ * ldg_closure_add_samples_coarse then takes one sample per coarse element
+ * with the coarse solver's own current state and gradient as features and
+ * P(K_f) - K_c(u_c) as target: after the coarse solver has run on its own
+ * from the projection, these are the states it produces itself, which is
+ * what an attached closure sees. */
+int ldg_closure_project_state(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse);
+int ldg_closure_add_samples_coarse(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse);
 int ldg_closure_sample_count(const ldg_closure* c, long long* count);
 /* Per-channel normalisation statistics from samples [first, first+count). */
 int ldg_closure_finalize_data(ldg_closure* c, long long first, long long count);

@@ -66,6 +66,10 @@ struct ldg_solver {
   double lo[3], hi[3];
   double p0 = 0, T0 = 0, R = 8.314, rho0 = 1.0, V0 = 1.0;
   cudaStream_t stream = nullptr;
+  // host <-> device state transfers: a copy stream and per-chunk events,
+  // made on first use (kXferChunks + 1 events)
+  cudaStream_t xfer = nullptr;
+  std::vector<cudaEvent_t> xev;
   // device buffers
   double *Un = nullptr, *Uacc = nullptr, *Us = nullptr, *Q = nullptr, *Tq = nullptr, *Fm = nullptr;
   double* Tu[2] = {nullptr, nullptr};
@@ -335,6 +339,9 @@ void free_all(ldg_solver* s) {
   if (s->Kadd) cudaFree(s->Kadd);
   for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
   s->ev.clear();
+  for (cudaEvent_t e : s->xev) cudaEventDestroy(e);
+  s->xev.clear();
+  if (s->xfer) cudaStreamDestroy(s->xfer);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -351,21 +358,6 @@ int dmalloc(ldg_solver* s, double** p, size_t count) {
 }
 
 size_t state_count(const ldg_solver* s) { return (size_t)s->nE * kNS * s->n; }
-
-int copy_in(ldg_solver* s, double* dst, const double* src, size_t count, int where) {
-  if (!src) return fail(LDG_ERR_INVALID, "null state pointer");
-  LDG_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
-                           where == LDG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream));
-  return LDG_OK;
-}
-
-int copy_out(ldg_solver* s, double* dst, const double* src, size_t count, int where) {
-  if (!dst) return fail(LDG_ERR_INVALID, "null output pointer");
-  LDG_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
-                           where == LDG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream));
-  if (where != LDG_DEVICE) LDG_CUDA(cudaStreamSynchronize(s->stream));
-  return LDG_OK;
-}
 
 // Event bracketing of launches (only when timing is enabled).
 cudaError_t tic(ldg_solver* s, int cls) {
@@ -450,6 +442,88 @@ cudaError_t s_rhs(ldg_solver* s, bool mixed, const StageCall& c) {
 
 // nodal (reference layout, in s->nodal) -> Un and the traces of Un; on the
 // mixed path also the FP32-pair copy of Un in Us (the stage-0 input).
+// Traces of elements [e0, e0+ne) only (each element's traces depend on its
+// own values alone).
+cudaError_t s_traces_range(ldg_solver* s, bool mixed, const double* U, void* Ucopy, double* Tu, int e0, int ne) {
+  const long per = (long)kNS * s->n, tper = 6L * kNS * s->nf;
+  double* uc = Ucopy ? static_cast<double*>(Ucopy) + e0 * per : nullptr;  // 8-byte values either way
+  if (mixed) LDG_DISPATCH(s->N, (launch_traces<NN, dd>(U + e0 * per, uc, Tu + e0 * tper, ne, s->odd, s->stream)));
+  LDG_DISPATCH(s->N, (launch_traces<NN, double>(U + e0 * per, uc, Tu + e0 * tper, ne, s->o64, s->stream)));
+}
+
+// Host <-> device state transfers are cut into kXferChunks element ranges:
+// the copy of one chunk (on the copy stream) overlaps the basis transform
+// and traces of the previous one (on the solver's stream).
+constexpr int kXferChunks = 8;
+
+int ensure_xfer(ldg_solver* s) {
+  if (s->xfer) return LDG_OK;
+  LDG_CUDA(cudaStreamCreateWithFlags(&s->xfer, cudaStreamNonBlocking));
+  s->xev.assign(kXferChunks + 1, nullptr);
+  for (auto& e : s->xev) LDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return LDG_OK;
+}
+
+void chunk_range(int nE, int c, int* e0, int* e1) {
+  *e0 = (int)((long)nE * c / kXferChunks);
+  *e1 = (int)((long)nE * (c + 1) / kXferChunks);
+}
+
+// A state in the reference layout (host or device) -> its Gauss values in U
+// on the solver's stream; with Tu also the traces of U (and, on the mixed
+// path, the pair copy Ucopy).  Host sources pass through s->nodal.
+int upload_gauss(ldg_solver* s, const double* u, int where, double* U, void* Ucopy, double* Tu, bool mixed) {
+  if (!u) return fail(LDG_ERR_INVALID, "null state pointer");
+  if (where == LDG_DEVICE) {
+    LDG_CUDA(d_transform(s->N, u, U, s->nE, s->ops, 0, s->stream));
+    if (Tu) LDG_CUDA(s_traces(s, mixed, U, Ucopy, Tu));
+    return LDG_OK;
+  }
+  int st = ensure_xfer(s);
+  if (st) return st;
+  const long per = (long)kNS * s->n;
+  // the copies start after the work already queued, which may read s->nodal
+  LDG_CUDA(cudaEventRecord(s->xev[kXferChunks], s->stream));
+  LDG_CUDA(cudaStreamWaitEvent(s->xfer, s->xev[kXferChunks], 0));
+  for (int c = 0; c < kXferChunks; ++c) {
+    int e0, e1;
+    chunk_range(s->nE, c, &e0, &e1);
+    if (e1 == e0) continue;
+    LDG_CUDA(cudaMemcpyAsync(s->nodal + e0 * per, u + e0 * per, (size_t)(e1 - e0) * per * sizeof(double),
+                             cudaMemcpyHostToDevice, s->xfer));
+    LDG_CUDA(cudaEventRecord(s->xev[c], s->xfer));
+    LDG_CUDA(cudaStreamWaitEvent(s->stream, s->xev[c], 0));
+    LDG_CUDA(d_transform(s->N, s->nodal + e0 * per, U + e0 * per, e1 - e0, s->ops, 0, s->stream));
+    if (Tu) LDG_CUDA(s_traces_range(s, mixed, U, Ucopy, Tu, e0, e1 - e0));
+  }
+  return LDG_OK;
+}
+
+// Gauss values U -> the reference layout in u (host or device).  Host
+// outputs pass through s->nodal; the call returns once they are on the host.
+int download_gauss(ldg_solver* s, const double* U, double* u, int where) {
+  if (!u) return fail(LDG_ERR_INVALID, "null output pointer");
+  if (where == LDG_DEVICE) {
+    LDG_CUDA(d_transform(s->N, U, u, s->nE, s->ops, 1, s->stream));
+    return LDG_OK;
+  }
+  int st = ensure_xfer(s);
+  if (st) return st;
+  const long per = (long)kNS * s->n;
+  for (int c = 0; c < kXferChunks; ++c) {
+    int e0, e1;
+    chunk_range(s->nE, c, &e0, &e1);
+    if (e1 == e0) continue;
+    LDG_CUDA(d_transform(s->N, U + e0 * per, s->nodal + e0 * per, e1 - e0, s->ops, 1, s->stream));
+    LDG_CUDA(cudaEventRecord(s->xev[c], s->stream));
+    LDG_CUDA(cudaStreamWaitEvent(s->xfer, s->xev[c], 0));
+    LDG_CUDA(cudaMemcpyAsync(u + e0 * per, s->nodal + e0 * per, (size_t)(e1 - e0) * per * sizeof(double),
+                             cudaMemcpyDeviceToHost, s->xfer));
+  }
+  LDG_CUDA(cudaStreamSynchronize(s->xfer));
+  return LDG_OK;
+}
+
 int load_state_from_nodal(ldg_solver* s) {
   LDG_CUDA(d_transform(s->N, s->nodal, s->Un, s->nE, s->ops, 0, s->stream));
   LDG_CUDA(s_traces(s, s->mixed, s->Un, s->mixed ? (void*)s->Us : nullptr, s->Tu[s->cur]));
@@ -941,34 +1015,25 @@ int ldg_set_initial_condition(ldg_solver* s) {
 int ldg_set_state(ldg_solver* s, const double* u, int where) {
   if (!s) return fail(LDG_ERR_INVALID, "null solver");
   LDG_CUDA(cudaSetDevice(s->cfg.device));
-  int st = copy_in(s, s->nodal, u, state_count(s), where);
-  if (st) return st;
-  return load_state_from_nodal(s);
+  return upload_gauss(s, u, where, s->Un, s->mixed ? (void*)s->Us : nullptr, s->Tu[s->cur], s->mixed);
 }
 
 int ldg_get_state(ldg_solver* s, double* u, int where) {
   if (!s) return fail(LDG_ERR_INVALID, "null solver");
   LDG_CUDA(cudaSetDevice(s->cfg.device));
-  LDG_CUDA(d_transform(s->N, s->Un, s->nodal, s->nE, s->ops, 1, s->stream));
-  return copy_out(s, u, s->nodal, state_count(s), where);
+  return download_gauss(s, s->Un, u, where);
 }
 
 int ldg_rhs(ldg_solver* s, const double* u_curr, double* k, int where) {
   if (!s) return fail(LDG_ERR_INVALID, "null solver");
   LDG_CUDA(cudaSetDevice(s->cfg.device));
-  int st = copy_in(s, s->nodal, u_curr, state_count(s), where);
-  if (st) return st;
   // Work in scratch buffers so the solver state (Un, Us, Tu[cur]) is kept:
-  // the FP64 input goes to Uacc, the stage-input copy to the nodal buffer.
+  // the FP64 input goes to Uacc, the stage-input pair copy (mixed path) to
+  // the nodal buffer.
   double* Tu = s->Tu[1 - s->cur];
-  LDG_CUDA(d_transform(s->N, s->nodal, s->Uacc, s->nE, s->ops, 0, s->stream));
-  const void* Uin = s->Uacc;
-  if (s->mixed) {
-    LDG_CUDA(s_traces(s, true, s->Uacc, s->nodal, Tu));
-    Uin = s->nodal;
-  } else {
-    LDG_CUDA(s_traces(s, false, s->Uacc, nullptr, Tu));
-  }
+  int st = upload_gauss(s, u_curr, where, s->Uacc, s->mixed ? (void*)s->nodal : nullptr, Tu, s->mixed);
+  if (st) return st;
+  const void* Uin = s->mixed ? (const void*)s->nodal : (const void*)s->Uacc;
   LDG_CUDA(s_grad(s, s->mixed, Uin, Tu, nullptr));
   StageCall c;
   if (s->closure) {  // the RHS the RK stages use: plain LDG plus the learned correction
@@ -984,10 +1049,10 @@ int ldg_rhs(ldg_solver* s, const double* u_curr, double* k, int where) {
   c.Kout = s->Us;  // FP64 RHS in the stage buffer (restored below on the mixed path)
   c.stage = -1;
   LDG_CUDA(s_rhs(s, s->mixed, c));
-  LDG_CUDA(d_transform(s->N, s->Us, s->nodal, s->nE, s->ops, 1, s->stream));
+  if ((st = download_gauss(s, s->Us, k, where))) return st;
   if (s->mixed)  // Us held the pair copy of Un: rebuild it
     LDG_CUDA(s_traces(s, true, s->Un, s->Us, s->Tu[1 - s->cur]));
-  return copy_out(s, k, s->nodal, state_count(s), where);
+  return LDG_OK;
 }
 
 int ldg_step(ldg_solver* s, int nsteps) {

@@ -8,6 +8,11 @@
 // projected state u_c.  One sample per coarse element:
 //   features  [u_c (5 x n), q (15 x n)]   (n = (p_c+1)^3 Gauss points)
 //   target    P(K_f) - K_c                (5 x n)
+// Solver in the loop (ldg_closure_project_state, then
+// ldg_closure_add_samples_coarse): the coarse solver starts from P(u_f),
+// runs on its own, and the samples take u_c from its state at the sample
+// time, with the target P(K_f) - K_c(u_c) -- the states the coarse solver
+// produces itself, which are what the closure sees when attached.
 // Network: x -> GELU(W1 x + b1) -> GELU(W2 h + b2) -> W3 h + b3, inputs and
 // outputs normalised per channel; BF16 weights and activations, FP32
 // accumulation on the tensor cores (ldg_mlp.cuh), FP32 master weights with
@@ -616,7 +621,16 @@ int ldg_closure_destroy(ldg_closure* c) {
   return LDG_OK;
 }
 
-int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse) {
+namespace {
+
+// What add_samples does with the coarse side.
+enum class SampleMode {
+  kProjected,  // features of the projected fine state (the coarse state is not touched)
+  kCoarse,     // features of the coarse solver's own current state
+  kSetState,   // no samples: the projected fine state becomes the coarse state
+};
+
+int add_samples_impl(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse, SampleMode mode) {
   if (!c || !fine || !coarse) return fail(LDG_ERR_INVALID, "closure: null argument");
   const SolverView f = solver_view(fine), k = solver_view(coarse);
   if (k.p != c->p) return fail(LDG_ERR_INVALID, "closure: coarse order differs");
@@ -626,9 +640,10 @@ int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse
   if (f.device != c->device || k.device != c->device) return fail(LDG_ERR_INVALID, "closure: devices differ");
   const int r = f.nx / k.nx, Nf = f.N, Nc = k.N;
   CL_CUDA(cudaSetDevice(c->device));
-  // everything below runs on the coarse solver's stream after the fine
-  // solver's queued work
+  // everything below runs on the coarse solver's stream after both
+  // solvers' queued work
   CL_CUDA(cudaStreamSynchronize(f.stream));
+  CL_CUDA(cudaStreamSynchronize(k.stream));
   cudaStream_t st = k.stream;
   const long fsz = (long)f.nE * 5 * f.n, csz = (long)k.nE * 5 * k.n;
   int rc;
@@ -644,10 +659,6 @@ int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse
     if ((rc = cl_alloc(&c->pc_U, csz)) || (rc = cl_alloc(&c->pc_KT, csz)) || (rc = cl_alloc(&c->pc_K, csz))) return rc;
     c->pc_cap = csz;
   }
-  // fine RHS of the fine state (Gauss basis)
-  if ((rc = solver_rhs_gauss(fine, f.Un, c->pf_K))) return rc;
-  CL_CUDA(cudaStreamSynchronize(f.stream));
-  // projections onto the coarse mesh
   std::vector<double> P1 = projection_1d(f.p, k.p, r);
   double* dP = nullptr;
   if ((rc = cl_alloc(&dP, P1.size()))) return rc;
@@ -655,10 +666,25 @@ int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse
   const int M = r * Nf;
   const size_t smem = sizeof(double) * 5 * ((size_t)M * M * M + (size_t)M * M * Nc + (size_t)M * Nc * Nc);
   CL_CUDA(cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_project<<<k.nE, 256, smem, st>>>(f.Un, c->pc_U, k.nx, k.ny, k.nz, r, Nf, Nc, 5, dP);
+  if (mode == SampleMode::kSetState) {
+    k_project<<<k.nE, 256, smem, st>>>(f.Un, c->pc_U, k.nx, k.ny, k.nz, r, Nf, Nc, 5, dP);
+    CL_CUDA(cudaGetLastError());
+    rc = solver_set_gauss_state(coarse, c->pc_U);
+    CL_CUDA(cudaStreamSynchronize(st));
+    cudaFree(dP);
+    return rc;
+  }
+  // fine RHS of the fine state (Gauss basis), projected onto the coarse mesh
+  if ((rc = solver_rhs_gauss(fine, f.Un, c->pf_K))) return rc;
+  CL_CUDA(cudaStreamSynchronize(f.stream));
   k_project<<<k.nE, 256, smem, st>>>(c->pf_K, c->pc_KT, k.nx, k.ny, k.nz, r, Nf, Nc, 5, dP);
+  // the state whose features the sample carries
+  if (mode == SampleMode::kProjected)
+    k_project<<<k.nE, 256, smem, st>>>(f.Un, c->pc_U, k.nx, k.ny, k.nz, r, Nf, Nc, 5, dP);
+  else
+    CL_CUDA(cudaMemcpyAsync(c->pc_U, k.Un, sizeof(double) * csz, cudaMemcpyDeviceToDevice, st));
   CL_CUDA(cudaGetLastError());
-  // coarse gradient and RHS of the projected state
+  // coarse gradient and RHS of that state
   if ((rc = solver_rhs_gauss(coarse, c->pc_U, c->pc_K))) return rc;
   if ((rc = ensure_samples(c, c->n_samples + k.nE))) return rc;
   const long total = (long)k.nE * c->in_dim;
@@ -670,6 +696,20 @@ int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse
   cudaFree(dP);
   c->n_samples += k.nE;
   return LDG_OK;
+}
+
+}  // namespace
+
+int ldg_closure_add_samples(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse) {
+  return add_samples_impl(c, fine, coarse, SampleMode::kProjected);
+}
+
+int ldg_closure_add_samples_coarse(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse) {
+  return add_samples_impl(c, fine, coarse, SampleMode::kCoarse);
+}
+
+int ldg_closure_project_state(ldg_closure* c, ldg_solver* fine, ldg_solver* coarse) {
+  return add_samples_impl(c, fine, coarse, SampleMode::kSetState);
 }
 
 int ldg_closure_sample_count(const ldg_closure* c, long long* count) {

@@ -161,6 +161,8 @@ SIGNATURES = {
     "ldg_closure_create": (_i, [_i, _i, ctypes.c_ulonglong, _i, ctypes.POINTER(_vp)]),
     "ldg_closure_destroy": (_i, [_vp]),
     "ldg_closure_add_samples": (_i, [_vp, _vp, _vp]),
+    "ldg_closure_project_state": (_i, [_vp, _vp, _vp]),
+    "ldg_closure_add_samples_coarse": (_i, [_vp, _vp, _vp]),
     "ldg_closure_sample_count": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
     "ldg_closure_finalize_data": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong]),
     "ldg_closure_train": (_i, [_vp, ctypes.c_longlong, ctypes.c_longlong, _i, _i, ctypes.c_float,
@@ -511,6 +513,15 @@ class Closure:
 
     def add_samples(self, fine: "Solver", coarse: "Solver") -> None:
         _check(load().ldg_closure_add_samples(self._h, fine._h, coarse._h), "ldg_closure_add_samples")
+
+    def project_state(self, fine: "Solver", coarse: "Solver") -> None:
+        """The coarse solver's state becomes the projection of the fine one's."""
+        _check(load().ldg_closure_project_state(self._h, fine._h, coarse._h), "ldg_closure_project_state")
+
+    def add_samples_coarse(self, fine: "Solver", coarse: "Solver") -> None:
+        """Samples with the coarse solver's own state as features (solver in
+        the loop) and P(K_f) - K_c(u_c) as target."""
+        _check(load().ldg_closure_add_samples_coarse(self._h, fine._h, coarse._h), "ldg_closure_add_samples_coarse")
 
     @property
     def samples(self) -> int:
