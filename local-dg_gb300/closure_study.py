@@ -91,17 +91,23 @@ class _Fine:
 
 def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iters=10000, batch=4096, lr=1e-3,
         hidden=128, amp=1e-2, data="projected", fine_precision="mixed", variants=None, device=0, log=None):
-    """The experiment; returns the summary and the KE series."""
+    """The experiment; returns the summary and the KE series.  Each variant
+    may name its own data set ("data": projected | loop | both; default the
+    `data` argument); every data set needed is collected from the same fine
+    runs, in a closure object of its own."""
     variants = variants or [{"name": "noise-0.3", "input_noise": 0.3, "lr_final": 0.05,
                              "modes": [["dissipative", 1.0, 10.0]]}]
+    for v in variants:
+        v.setdefault("data", data)
+    kinds = sorted({v["data"] for v in variants})
     say = log or (lambda *a: None)
     res = {"config": {"coarse": f"{coarse_nx}^3 p={P_COARSE} FP64, CFL 0.01",
                       "fine": f"{fine_nx}^3 p={P_FINE} {fine_precision}, CFL {fine_cfl}",
-                      "t_end": t_end, "sample_dt": sample_dt, "iters": iters, "data": data,
+                      "t_end": t_end, "sample_dt": sample_dt, "iters": iters, "data": kinds,
                       "seeds": {"train": [[SEED_TRAIN, 0], [SEED_TRAIN, 1]], "eval": [SEED_EVAL, 0]}}}
     series = {}
-    closure = ldg.Closure(p=P_COARSE, hidden=hidden, seed=7, device=device)
-    theta0 = closure.get_params()
+    closures = {k: ldg.Closure(p=P_COARSE, hidden=hidden, seed=7, device=device) for k in kinds}
+    theta0 = closures[kinds[0]].get_params()
     coarse_ws = ldg.Solver(P_COARSE, coarse_nx, steps=10, device=device)
     fine_view = ldg.Solver(P_FINE, fine_nx, steps=10, device=device) if fine_precision != "fp64" else None
 
@@ -115,17 +121,19 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
     # ---- training data: two fine runs (seed SEED_TRAIN, instances 0 and 1)
     t0 = time.perf_counter()
     fines = [_Fine(fine_nx, fine_steps, fine_cfl, amp, SEED_TRAIN, i, fine_precision, fine_view) for i in (0, 1)]
-    loops = [ldg.Solver(P_COARSE, coarse_nx, steps=10, device=device) for _ in fines] \
-        if data in ("loop", "both") else []
+    need_loop = any(k in ("loop", "both") for k in kinds)
+    loops = [ldg.Solver(P_COARSE, coarse_nx, steps=10, device=device) for _ in fines] if need_loop else []
+    any_c = closures[kinds[0]]
     for k in range(n_times):
         for m, f in enumerate(fines):
             fv = f.fp64()
-            if data in ("projected", "both"):
-                closure.add_samples(fv, coarse_ws)
+            for kind, c in closures.items():
+                if kind in ("projected", "both"):
+                    c.add_samples(fv, coarse_ws)
+                if kind in ("loop", "both") and k > 0:
+                    c.add_samples_coarse(fv, loops[m])
             if loops:
-                if k > 0:
-                    closure.add_samples_coarse(fv, loops[m])
-                closure.project_state(fv, loops[m])
+                any_c.project_state(fv, loops[m])
         if k + 1 < n_times:
             for f in fines:
                 f.s.step(per_sample)
@@ -135,7 +143,7 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
         f.close()
     for c in loops:
         c.close()
-    n_train = closure.samples
+    n_train = {kind: c.samples for kind, c in closures.items()}
     res["train_runs"] = {"steps": (n_times - 1) * per_sample, "dt": dt_f, "sample_every_steps": per_sample,
                          "sample_times": n_times, "samples": n_train, "seconds": time.perf_counter() - t0}
     say("training data", res["train_runs"])
@@ -144,7 +152,9 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
     t0 = time.perf_counter()
     ev = _Fine(fine_nx, fine_steps, fine_cfl, amp, SEED_EVAL, 0, fine_precision, fine_view)
     for k in range(n_times):
-        closure.add_samples(ev.fp64(), coarse_ws)
+        fv = ev.fp64()
+        for c in closures.values():
+            c.add_samples(fv, coarse_ws)
         if k + 1 < n_times:
             ev.s.step(per_sample)
     ev.s.step(fine_steps - (n_times - 1) * per_sample)
@@ -152,19 +162,20 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
     ev.close()
     if fine_view is not None:
         fine_view.close()
-    n_held = closure.samples - n_train
+    n_held = {kind: c.samples - n_train[kind] for kind, c in closures.items()}
     res["eval_run"] = {"steps": fine_steps, "dt": dt_f, "seconds": time.perf_counter() - t0}
     say("evaluation run", res["eval_run"])
 
     # ---- a posteriori reference: the plain coarse LDG run
-    closure.finalize(0, n_train)
+    for kind, c in closures.items():
+        c.finalize(0, n_train[kind])
     nc_steps = int(math.ceil(t_end / dt_c))
 
-    def coarse_run(name, attach):
+    def coarse_run(name, closure):
         t0 = time.perf_counter()
         with ldg.Solver(P_COARSE, coarse_nx, steps=nc_steps, perturb_amp=amp, seed=SEED_EVAL, instance=0,
                         device=device) as s:
-            if attach:
+            if closure is not None:
                 s.attach_closure(closure)
             status, done = "ok", 0
             try:
@@ -181,32 +192,36 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
 
     tf_, ef = dissipation(series["ke_fine"], dt_f)
     scale = float(np.max(ef))
-    info = coarse_run("plain", False)
+    info = coarse_run("plain", None)
     summary = {"fine": compare(series["ke_fine"], dt_f, tf_, ef, scale),
                "plain": dict(compare(series["ke_plain"], info["dt"], tf_, ef, scale), **info)}
     res["a_posteriori"] = summary
     res["training"], res["a_priori"] = {}, {}
     for var in variants:
-        vn = var["name"]
+        vn, closure = var["name"], closures[var["data"]]
         t0 = time.perf_counter()
         closure.set_params(theta0)
         closure.set_options(input_noise=float(var.get("input_noise", 0.0)), lr_final=float(var.get("lr_final", 1.0)))
-        losses = closure.train(0, n_train, iters=iters, batch=batch, lr=lr, seed=3)
-        e_plain, e_closure = closure.evaluate(n_train, n_held)
-        res["training"][vn] = {"seconds": time.perf_counter() - t0, "samples": n_train,
+        nt = n_train[var["data"]]
+        losses = closure.train(0, nt, iters=iters, batch=batch, lr=lr, seed=3)
+        e_plain, e_closure = closure.evaluate(nt, n_held[var["data"]])
+        res["training"][vn] = {"data": var["data"], "seconds": time.perf_counter() - t0, "samples": nt,
                                "loss_first50": float(np.mean(losses[:50])), "loss_last50": float(np.mean(losses[-50:]))}
-        res["a_priori"][vn] = {"heldout_samples": n_held, "rhs_err_plain": e_plain, "rhs_err_closure": e_closure}
+        res["a_priori"][vn] = {"heldout_samples": n_held[var["data"]], "rhs_err_plain": e_plain,
+                               "rhs_err_closure": e_closure}
         for mode in var["modes"]:
             energy, fac = mode[0], float(mode[1])
             ood = float(mode[2]) if len(mode) > 2 else 10.0
             name = f"{vn}/{energy}/x{fac:g}/ood{ood:g}"
             closure.set_options(energy=energy, scale=fac, ood_sigma=ood)
             f0, c0 = closure.fallbacks, closure.clipped
-            info = coarse_run(name, True)
+            info = coarse_run(name, closure)
             summary[name] = dict(compare(series["ke_" + name], info["dt"], tf_, ef, scale), **info)
+            summary[name]["data"] = var["data"]
             summary[name]["fallback_element_stages"] = closure.fallbacks - f0
             summary[name]["projected_element_stages"] = closure.clipped - c0
             say(name, summary[name])
-    closure.close()
+    for c in closures.values():
+        c.close()
     coarse_ws.close()
     return res, series

@@ -15,8 +15,8 @@ of FP64).
 Usage:
     python local-dg_gb300/examples/closure_tgv.py --out results.json \\
         [--t-end 20] [--sample-dt 0.5] [--iters 10000] [--data projected|loop|both] \\
-        [--variants '[{"name": ..., "input_noise": 0.3, "lr_final": 0.05,
-                       "modes": [["dissipative", 1.0, 10.0]]}]']
+        [--variants '[{"name": ..., "data": "loop", "input_noise": 0.3, "lr_final": 0.05,
+                       "modes": [["dissipative", 1.0, 10.0]]}]' | --variants @closure_c5_variants.json]
 
 Writes the JSON summary and the KE series (<out>.npz).
 """
@@ -49,14 +49,26 @@ def main():
     ap.add_argument("--fine-nx", type=int, default=32)
     ap.add_argument("--data", default="projected", choices=["projected", "loop", "both"])
     ap.add_argument("--fine-precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--variants", default=None, help="JSON list of closure variants")
+    ap.add_argument("--variants", default=None,
+                    help="JSON list of closure variants, or @file with one (e.g. @closure_c5_variants.json)")
     args = ap.parse_args()
+    variants = None
+    if args.variants:
+        if args.variants.startswith("@"):
+            path = args.variants[1:]
+            if not os.path.isabs(path) and not os.path.exists(path):
+                path = os.path.join(HERE, path)
+            with open(path) as f:
+                variants = json.load(f)
+        else:
+            variants = json.loads(args.variants)
     res, series = closure_study.run(
         coarse_nx=args.coarse_nx, fine_nx=args.fine_nx, t_end=args.t_end, sample_dt=args.sample_dt,
         fine_cfl=args.fine_cfl, iters=args.iters, batch=args.batch, lr=args.lr, hidden=args.hidden, amp=args.amp,
         data=args.data, fine_precision=args.fine_precision,
-        variants=json.loads(args.variants) if args.variants else None,
+        variants=variants,
         log=lambda *a: print(*a, file=sys.stderr, flush=True))
+    res["command"] = " ".join(["python", "local-dg_gb300/examples/closure_tgv.py"] + sys.argv[1:])
     with open(args.out, "w") as f:
         json.dump(res, f, indent=1)
     np.savez(os.path.splitext(args.out)[0] + ".npz", **series)
