@@ -443,24 +443,30 @@ def run_ours(args):
         s.get_state(host)
     e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
     assert np.all(np.isfinite(host))
-    # where an end-to-end step goes (untimed diagnostic: each call waited for)
-    parts = {"set_state": [], "step": [], "get_state": []}
-    for _ in range(3):
-        t = time.perf_counter()
-        s.set_state(host)
-        s.synchronize()
-        parts["set_state"].append(time.perf_counter() - t)
-        t = time.perf_counter()
-        s.step(1)
-        s.synchronize()
-        parts["step"].append(time.perf_counter() - t)
-        t = time.perf_counter()
-        s.get_state(host)
-        parts["get_state"].append(time.perf_counter() - t)
+    # where an end-to-end step goes (untimed diagnostic: each call waited
+    # for), with the transfers overlapped with the transforms in 8 chunks
+    # (the default) and copied whole before transforming (1 chunk)
+    breakdown = {}
+    for chunks in (8, 1):
+        s.set_transfer_chunks(chunks)
+        parts = {"set_state": [], "step": [], "get_state": []}
+        for _ in range(3):
+            t = time.perf_counter()
+            s.set_state(host)
+            s.synchronize()
+            parts["set_state"].append(time.perf_counter() - t)
+            t = time.perf_counter()
+            s.step(1)
+            s.synchronize()
+            parts["step"].append(time.perf_counter() - t)
+            t = time.perf_counter()
+            s.get_state(host)
+            parts["get_state"].append(time.perf_counter() - t)
+        breakdown[f"chunks_{chunks}"] = {k: 1e3 * sorted(v)[1] for k, v in parts.items()}
+    s.set_transfer_chunks(8)
     e2e = {"value": ws * n_per_step * Ke / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes, "steps": Ke,
-           "ms_per_step": e2e_s * 1e3 / Ke,
-           "breakdown_ms": {k: 1e3 * sorted(v)[1] for k, v in parts.items()}}
+           "ms_per_step": e2e_s * 1e3 / Ke, "breakdown_ms": breakdown}
 
     # ---- roofline of the dominant kernel (live event timings above)
     hbm_peak, peak_kind = read_peaks()

@@ -120,6 +120,11 @@ int ldg_get_info(const ldg_solver* s, ldg_info* info);
  * layout; where = LDG_HOST or LDG_DEVICE. */
 int ldg_set_state(ldg_solver* s, const double* u, int where);
 int ldg_get_state(ldg_solver* s, double* u, int where);
+/* Host buffers (in ldg_set_state, ldg_get_state, ldg_rhs) move in `chunks`
+ * element ranges (1..64, default 8) on a copy stream, so that the copy of
+ * one range overlaps the basis transform of the previous one; 1 copies the
+ * whole state before transforming it.  (No reference counterpart.) */
+int ldg_set_transfer_chunks(ldg_solver* s, int chunks);
 
 /* Resets the state to the Taylor-Green vortex (solver.cpp:194-236) and the
  * step counter to 0. */

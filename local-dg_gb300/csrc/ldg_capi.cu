@@ -67,9 +67,10 @@ struct ldg_solver {
   double p0 = 0, T0 = 0, R = 8.314, rho0 = 1.0, V0 = 1.0;
   cudaStream_t stream = nullptr;
   // host <-> device state transfers: a copy stream and per-chunk events,
-  // made on first use (kXferChunks + 1 events)
+  // made on first use (kMaxXferChunks + 1 events)
   cudaStream_t xfer = nullptr;
   std::vector<cudaEvent_t> xev;
+  int xfer_chunks = 8;  // ldg_set_transfer_chunks
   // device buffers
   double *Un = nullptr, *Uacc = nullptr, *Us = nullptr, *Q = nullptr, *Tq = nullptr, *Fm = nullptr;
   double* Tu[2] = {nullptr, nullptr};
@@ -451,22 +452,22 @@ cudaError_t s_traces_range(ldg_solver* s, bool mixed, const double* U, void* Uco
   LDG_DISPATCH(s->N, (launch_traces<NN, double>(U + e0 * per, uc, Tu + e0 * tper, ne, s->o64, s->stream)));
 }
 
-// Host <-> device state transfers are cut into kXferChunks element ranges:
-// the copy of one chunk (on the copy stream) overlaps the basis transform
-// and traces of the previous one (on the solver's stream).
-constexpr int kXferChunks = 8;
+// Host <-> device state transfers are cut into s->xfer_chunks element
+// ranges: the copy of one chunk (on the copy stream) overlaps the basis
+// transform and traces of the previous one (on the solver's stream).
+constexpr int kMaxXferChunks = 64;
 
 int ensure_xfer(ldg_solver* s) {
   if (s->xfer) return LDG_OK;
   LDG_CUDA(cudaStreamCreateWithFlags(&s->xfer, cudaStreamNonBlocking));
-  s->xev.assign(kXferChunks + 1, nullptr);
+  s->xev.assign(kMaxXferChunks + 1, nullptr);
   for (auto& e : s->xev) LDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   return LDG_OK;
 }
 
-void chunk_range(int nE, int c, int* e0, int* e1) {
-  *e0 = (int)((long)nE * c / kXferChunks);
-  *e1 = (int)((long)nE * (c + 1) / kXferChunks);
+void chunk_range(int nE, int chunks, int c, int* e0, int* e1) {
+  *e0 = (int)((long)nE * c / chunks);
+  *e1 = (int)((long)nE * (c + 1) / chunks);
 }
 
 // A state in the reference layout (host or device) -> its Gauss values in U
@@ -483,11 +484,11 @@ int upload_gauss(ldg_solver* s, const double* u, int where, double* U, void* Uco
   if (st) return st;
   const long per = (long)kNS * s->n;
   // the copies start after the work already queued, which may read s->nodal
-  LDG_CUDA(cudaEventRecord(s->xev[kXferChunks], s->stream));
-  LDG_CUDA(cudaStreamWaitEvent(s->xfer, s->xev[kXferChunks], 0));
-  for (int c = 0; c < kXferChunks; ++c) {
+  LDG_CUDA(cudaEventRecord(s->xev[kMaxXferChunks], s->stream));
+  LDG_CUDA(cudaStreamWaitEvent(s->xfer, s->xev[kMaxXferChunks], 0));
+  for (int c = 0; c < s->xfer_chunks; ++c) {
     int e0, e1;
-    chunk_range(s->nE, c, &e0, &e1);
+    chunk_range(s->nE, s->xfer_chunks, c, &e0, &e1);
     if (e1 == e0) continue;
     LDG_CUDA(cudaMemcpyAsync(s->nodal + e0 * per, u + e0 * per, (size_t)(e1 - e0) * per * sizeof(double),
                              cudaMemcpyHostToDevice, s->xfer));
@@ -510,9 +511,9 @@ int download_gauss(ldg_solver* s, const double* U, double* u, int where) {
   int st = ensure_xfer(s);
   if (st) return st;
   const long per = (long)kNS * s->n;
-  for (int c = 0; c < kXferChunks; ++c) {
+  for (int c = 0; c < s->xfer_chunks; ++c) {
     int e0, e1;
-    chunk_range(s->nE, c, &e0, &e1);
+    chunk_range(s->nE, s->xfer_chunks, c, &e0, &e1);
     if (e1 == e0) continue;
     LDG_CUDA(d_transform(s->N, U + e0 * per, s->nodal + e0 * per, e1 - e0, s->ops, 1, s->stream));
     LDG_CUDA(cudaEventRecord(s->xev[c], s->stream));
@@ -1010,6 +1011,15 @@ int ldg_set_initial_condition(ldg_solver* s) {
   LDG_CUDA(launch_initial_condition(pb, s->nodal, s->stream));
   s->step = 0;
   return load_state_from_nodal(s);
+}
+
+int ldg_set_transfer_chunks(ldg_solver* s, int chunks) {
+  if (!s || chunks < 1 || chunks > kMaxXferChunks) return fail(LDG_ERR_INVALID, "transfer chunks must be 1..64");
+  LDG_CUDA(cudaSetDevice(s->cfg.device));
+  LDG_CUDA(cudaStreamSynchronize(s->stream));
+  if (s->xfer) LDG_CUDA(cudaStreamSynchronize(s->xfer));
+  s->xfer_chunks = chunks;
+  return LDG_OK;
 }
 
 int ldg_set_state(ldg_solver* s, const double* u, int where) {

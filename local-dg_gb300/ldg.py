@@ -146,6 +146,7 @@ SIGNATURES = {
     "ldg_probe_fp64_peak": (_i, [_i, _dp]),
     "ldg_probe_fp64": (_i, [_i, _dp, _dp, _dp]),
     "ldg_probe_contraction": (_i, [_vp, _i, _i, _dp, _dp]),
+    "ldg_set_transfer_chunks": (_i, [_vp, _i]),
     "ldg_rhs_noalloc": (_i, [ctypes.POINTER(LdgConfig), _vp, _vp, _vp]),
     "ldg_ensemble_create": (_i, [ctypes.POINTER(LdgConfig), _i, ctypes.POINTER(_vp)]),
     "ldg_ensemble_destroy": (_i, [_vp]),
@@ -337,6 +338,11 @@ class Solver:
         if where == LDG_DEVICE:
             self.synchronize()
         del keep
+
+    def set_transfer_chunks(self, chunks: int) -> None:
+        """Host transfers in `chunks` element ranges overlapped with the basis
+        transforms (1: copy everything, then transform)."""
+        _check(load().ldg_set_transfer_chunks(self._h, chunks), "ldg_set_transfer_chunks")
 
     def get_state(self, out=None):
         if out is None:

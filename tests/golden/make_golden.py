@@ -94,63 +94,87 @@ def series(threads: int = 8):
             print(f"series_n{nx}_p{p}: {m['seconds']:.1f} s", flush=True)
 
 
-def series_64(threads: int = 8, ref_steps: int = 20, steps: int = 200, ens_every_ref: int = 4,
-              ens_every: int = 10, ref_dir: str | None = None):
-    """The 64^3 p=4 fixture: the reference's first ref_steps steps pin the
-    factored oracle, which then provides all `steps` steps.  ref_dir may
-    hold an earlier reference run's output (ser.ke, ser.norms, ser.samples,
-    ser.enst, ser.meta of `ldg_ref series 64 4 <ref_steps> ser idx <threads>
-    <ens_every_ref>` with the same seeded idx); otherwise it is run here."""
-    nx, p, count, seed = 64, 4, 4096, 64
-    nU = (p + 1) ** 3 * 5 * nx ** 3
-    ref_idx = np.sort(np.random.default_rng(seed).choice(nU, count, replace=False)).astype(np.int64)
-    idx = ref_idx[::4].copy()
+SERIES64 = dict(nx=64, p=4, count=4096, seed=64, ref_steps=20, steps=200, ens_every_ref=4, ens_every=10)
+
+
+def series64_indices():
+    c = SERIES64
+    nU = (c["p"] + 1) ** 3 * 5 * c["nx"] ** 3
+    ref_idx = np.sort(np.random.default_rng(c["seed"]).choice(nU, c["count"], replace=False)).astype(np.int64)
+    return ref_idx, ref_idx[::4].copy()
+
+
+def series64_oracle(out_npz: str, threads: int = 8):
+    """Phase 1 of the 64^3 p=4 fixture: the oracle's factored chain over all
+    steps, recording per step the KE, norms and the entries at the 4096
+    reference sample indices, and the enstrophy at every step that the
+    reference window or the fixture records it."""
+    c = SERIES64
+    ref_idx, _ = series64_indices()
+    o = oracle.Oracle(c["nx"], c["p"], steps=c["steps"], threads=threads)
+    o.set_factored(True)
+    u = o.initial_condition()
+    ke, norms, samples, enst, enst_steps = [], [], [], [], []
+    for k in range(1, c["steps"] + 1):
+        u, kk = o.step(u, 1)
+        ke.append(kk[0])
+        norms.append(np.einsum("evq,evq->v", u, u))
+        samples.append(u.ravel()[ref_idx])
+        if k % c["ens_every"] == 0 or (k <= c["ref_steps"] and k % c["ens_every_ref"] == 0):
+            enst.append(o.enstrophy(u))
+            enst_steps.append(k)
+        if k % 10 == 0:
+            print(f"series_n64_p4 oracle: step {k}", flush=True)
+    np.savez(out_npz, ke=np.array(ke), norms=np.array(norms), samples=np.array(samples), enst=np.array(enst),
+             enst_steps=np.array(enst_steps), dt=o.dt, threads=threads)
+
+
+def series_64(threads: int = 8, ref_dir: str | None = None, oracle_npz: str | None = None):
+    """The 64^3 p=4 fixture: the reference's first ref_steps steps (run
+    here, or read from ref_dir: the output of `ldg_ref series 64 4 20 ser
+    idx <threads> 4` with the seeded indices of series64_indices) pin the
+    oracle's factored chain (phase 1, run here or read from oracle_npz),
+    which then provides all steps."""
+    c = SERIES64
+    ref_idx, idx = series64_indices()
     with tempfile.TemporaryDirectory() as tmp:
         if ref_dir is None:
             if not os.path.exists(oracle.REF_BIN):
                 subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
             ref_idx.tofile(os.path.join(tmp, "idx"))
-            oracle.run_reference(["series", nx, p, ref_steps, "ser", "idx", threads, ens_every_ref], tmp)
+            oracle.run_reference(["series", c["nx"], c["p"], c["ref_steps"], "ser", "idx", threads,
+                                  c["ens_every_ref"]], tmp)
             ref_dir = tmp
         m = meta(os.path.join(ref_dir, "ser.meta"))
-        assert int(m["steps"]) == ref_steps and int(m["nx"]) == nx and int(m["p"]) == p
+        assert int(m["steps"]) == c["ref_steps"] and int(m["nx"]) == c["nx"] and int(m["p"]) == c["p"]
+        R = c["ref_steps"]
         ref_ke = np.fromfile(os.path.join(ref_dir, "ser.ke"))
-        ref_norms = np.fromfile(os.path.join(ref_dir, "ser.norms")).reshape(ref_steps, 5)
-        ref_samples = np.fromfile(os.path.join(ref_dir, "ser.samples")).reshape(ref_steps, count)
+        ref_norms = np.fromfile(os.path.join(ref_dir, "ser.norms")).reshape(R, 5)
+        ref_samples = np.fromfile(os.path.join(ref_dir, "ser.samples")).reshape(R, c["count"])
         ref_e = np.fromfile(os.path.join(ref_dir, "ser.enst")).reshape(-1, 2)
-    o = oracle.Oracle(nx, p, steps=steps, threads=threads)
-    o.set_factored(True)
-    assert abs(o.dt - m["dt"]) <= 1e-15 * m["dt"]
-    u = o.initial_condition()
-    ke, norms, samples, enst, enst_steps = [], [], [], [], []
-    ref_enst = dict((int(k), v) for k, v in ref_e)
-    for k in range(1, steps + 1):
-        u, kk = o.step(u, 1)
-        ke.append(kk[0])
-        flat = u.ravel()
-        nrm = np.einsum("evq,evq->v", u, u)
-        norms.append(nrm)
-        samples.append(flat[idx])
-        if k % ens_every == 0 or k in ref_enst:
-            enst.append(o.enstrophy(u))
-            enst_steps.append(k)
-        if k <= ref_steps:  # the pin: every step of the reference window
-            tot = np.sqrt(np.sum(ref_norms[k - 1]))
-            e_ke = abs(kk[0] - ref_ke[k - 1]) / ref_ke[k - 1]
-            e_s = np.linalg.norm(flat[ref_idx] - ref_samples[k - 1]) / np.linalg.norm(ref_samples[k - 1])
-            e_n = np.max(np.abs(np.sqrt(nrm) - np.sqrt(ref_norms[k - 1]))) / tot
-            assert e_ke <= 1e-12 and e_s <= 1e-12 and e_n <= 1e-12, (k, e_ke, e_s, e_n)
-            if k in ref_enst:
-                e_e = abs(enst[-1] - ref_enst[k]) / ref_enst[k]
-                assert e_e <= 1e-12, (k, e_e)
-        if k % 10 == 0:
-            print(f"series_n64_p4: step {k}", flush=True)
-    np.savez_compressed(os.path.join(HERE, "series_n64_p4.npz"), idx=idx, ke=np.array(ke),
-                        norms=np.array(norms), samples=np.array(samples), dt=o.dt, steps=steps, ke0=m["ke0"],
-                        enst=np.array(enst), enst_steps=np.array(enst_steps),
+        if oracle_npz is None:
+            oracle_npz = os.path.join(tmp, "oracle.npz")
+            series64_oracle(oracle_npz, threads)
+        z = np.load(oracle_npz)
+    assert abs(float(z["dt"]) - m["dt"]) <= 1e-15 * m["dt"]
+    ens = dict(zip(z["enst_steps"].tolist(), z["enst"].tolist()))
+    for k in range(1, R + 1):  # the pin: every step of the reference window
+        tot = np.sqrt(np.sum(ref_norms[k - 1]))
+        e_ke = abs(z["ke"][k - 1] - ref_ke[k - 1]) / ref_ke[k - 1]
+        e_s = np.linalg.norm(z["samples"][k - 1] - ref_samples[k - 1]) / np.linalg.norm(ref_samples[k - 1])
+        e_n = np.max(np.abs(np.sqrt(z["norms"][k - 1]) - np.sqrt(ref_norms[k - 1]))) / tot
+        assert e_ke <= 1e-12 and e_s <= 1e-12 and e_n <= 1e-12, (k, e_ke, e_s, e_n)
+    for k, v in ref_e:
+        assert abs(ens[int(k)] - v) <= 1e-12 * abs(v), (k, ens[int(k)], v)
+    keep = np.searchsorted(ref_idx, idx)
+    fix = [k for k in sorted(ens) if k % c["ens_every"] == 0]
+    np.savez_compressed(os.path.join(HERE, "series_n64_p4.npz"), idx=idx, ke=z["ke"], norms=z["norms"],
+                        samples=z["samples"][:, keep], dt=z["dt"], steps=c["steps"], ke0=m["ke0"],
+                        enst=np.array([ens[k] for k in fix]), enst_steps=np.array(fix),
                         ref_idx=ref_idx, ref_ke=ref_ke, ref_norms=ref_norms, ref_samples=ref_samples,
                         ref_enst=ref_e[:, 1], ref_enst_steps=ref_e[:, 0].astype(np.int64),
-                        ref_steps=ref_steps, ref_seconds=m["seconds"], threads=threads)
+                        ref_steps=R, ref_seconds=m["seconds"], threads=threads)
+    print("series_n64_p4: pinned to the reference's window and written", flush=True)
 
 
 def main():
@@ -158,8 +182,12 @@ def main():
         series()
         series_64()
         return
-    if len(sys.argv) > 1 and sys.argv[1] == "series64":  # [ref_dir]
-        series_64(ref_dir=sys.argv[2] if len(sys.argv) > 2 else None)
+    if len(sys.argv) > 1 and sys.argv[1] == "series64-oracle":  # <out.npz>: phase 1 alone
+        series64_oracle(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "series64":  # [ref_dir [oracle.npz]]
+        series_64(ref_dir=sys.argv[2] if len(sys.argv) > 2 else None,
+                  oracle_npz=sys.argv[3] if len(sys.argv) > 3 else None)
         return
     if not os.path.exists(oracle.REF_BIN):
         subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
