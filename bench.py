@@ -375,9 +375,21 @@ def learned_variant(K, W, dev):
     try:
         with open(CLOSURE_RECORD) as f:
             rec = json.load(f)
-        out["recorded_a_posteriori"] = {"source": os.path.relpath(CLOSURE_RECORD, ROOT),
-                                        "config": rec.get("config"), "a_posteriori": rec.get("a_posteriori")}
-    except OSError:
+        ap = rec["a_posteriori"]
+        keys = ("rms_err_rel", "max_err_rel", "final_ke", "peak_time")
+        runs = {k: v for k, v in ap.items() if k not in ("fine", "plain") and v.get("rms_err_rel") is not None}
+        best = min(runs, key=lambda k: runs[k]["rms_err_rel"])
+        out["recorded_a_posteriori"] = {
+            "source": os.path.relpath(CLOSURE_RECORD, ROOT), "command": rec.get("command"),
+            "config": rec.get("config"),
+            "metric": "KE-dissipation-rate error (solver.cpp:438-440) vs the fine run, t >= 1, rel. to its peak",
+            "fine": {k: ap["fine"].get(k) for k in ("final_ke", "peak_time")},
+            "plain": {k: ap["plain"].get(k) for k in keys},
+            "best_closure": dict({k: runs[best].get(k) for k in keys}, variant=best,
+                                 fallback_element_stages=runs[best].get("fallback_element_stages")),
+            "closure_beats_plain": runs[best]["rms_err_rel"] < ap["plain"]["rms_err_rel"],
+            "variants_tried": len(runs)}
+    except (OSError, KeyError, ValueError):
         out["recorded_a_posteriori"] = None
     return out
 
