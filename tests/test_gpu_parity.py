@@ -195,3 +195,30 @@ def test_time_step_runs_to_tf():
         info = s.info()
         assert info.step == 6 == s.timesteps
         assert s.ke_history().shape == (6,)
+
+
+@pytest.mark.gpu
+def test_transfer_chunking_changes_no_bit():
+    """Host transfers overlapped with the basis transforms in element chunks
+    (ldg_set_transfer_chunks) give the same bits as one whole copy: the
+    state round trip, a step, and an RHS through host buffers, for 1, 3, 8
+    and 64 chunks on a mesh whose element count 64 does not divide evenly."""
+    rng = np.random.default_rng(4)
+    with ldg.Solver(3, 4, 4, 5, steps=3) as s:  # 80 elements
+        u0 = s.get_state()
+        u0[:, 1:4] += 0.01 * rng.standard_normal(u0[:, 1:4].shape)
+        outs = []
+        for chunks in (1, 3, 8, 64):
+            s.set_transfer_chunks(chunks)
+            s.set_state(u0)
+            back = s.get_state()
+            k = s.rhs(u0)
+            s.step(1)
+            outs.append((back, k, s.get_state()))
+    for back, k, u1 in outs[1:]:
+        assert np.array_equal(back, outs[0][0])
+        assert np.array_equal(k, outs[0][1])
+        assert np.array_equal(u1, outs[0][2])
+    with pytest.raises(ldg.LdgError):
+        with ldg.Solver(2, 3) as s:
+            s.set_transfer_chunks(0)
