@@ -115,3 +115,18 @@ def test_contraction_arithmetics_against_fp64(mode, tol):
     assert err <= tol, (mode, err)
     if mode == "tensor_core_slices":
         assert err > 1e-13  # it is the sliced arithmetic that ran, not FP64
+
+
+def test_mixed_vs_reference_series_32_p3_200_steps():
+    """The mixed path against the reference's own Taylor-Green run at 32^3
+    p=3 (tests/golden/series_n32_p3.npz): after 200 RK4 steps the sampled
+    state entries within the mixed bar, and the KE series within 1e-10."""
+    z = np.load(os.path.join(GOLDEN, "series_n32_p3.npz"))
+    steps = int(z["steps"])
+    with ldg.Solver(3, 32, steps=steps, precision="mixed") as s:
+        assert abs(s.dt - float(z["dt"])) <= 1e-15 * float(z["dt"])
+        s.step(steps)
+        u = s.get_state()
+        ke = s.ke_history()
+    assert rel_l2(u.ravel()[z["idx"]], z["samples"][-1]) <= MIXED_TOL
+    assert np.max(np.abs(ke - z["ke"]) / z["ke"]) <= 1e-10
