@@ -184,9 +184,9 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_traces(const double* __restrict__
 // Writes Q and the minus-face traces Tq; on the FP64 path optionally the
 // per-element enstrophy.
 // Shared memory of grad_body, in 8-byte values per element: U (5n), the +l
-// traces of the element and of its -l neighbours (2 x 15 nf), Q (15 n) and
-// the enstrophy density (n).  The Roe flux reads the element's own -l
-// traces from global memory (where the previous pass wrote them).
+// traces of the element and of its -l neighbours (2 x 15 nf), the element's
+// own -l traces (15 nf, needed by the Roe phase only) whose space Q (15 n)
+// reuses after that phase, and the enstrophy density (n).
 template <int N>
 constexpr int grad_smem_values_per_element() {
   return kNS * N * N * N + 2 * 3 * kNS * N * N + kNQ * N * N * N + N * N * N;
@@ -202,11 +202,12 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
                                           double* smem_raw) {
   constexpr int n = Cfg<N, E>::n, nf = Cfg<N, E>::nf, EPC = Cfg<N, E>::EPC, NT = Cfg<N, E>::T;
   using R = Real<T>;
-  __shared__ int s_next;                   // the work list's counter
+  static_assert(kNQ * n >= 3 * kNS * nf, "Q must cover the -l trace space it reuses");
   T* sU = reinterpret_cast<T*>(smem_raw);  // EPC*5*n
   T* sTp = sU + EPC * kNS * n;             // EPC*3*5*nf  own +l traces
   T* sTm = sTp + EPC * 3 * kNS * nf;       // EPC*3*5*nf  (-l neighbour)'s +l traces
-  T* sQ = sTm + EPC * 3 * kNS * nf;        // EPC*15*n
+  T* sTo = sTm + EPC * 3 * kNS * nf;       // EPC*3*5*nf  own -l traces (Roe phase)
+  T* sQ = sTo;                             // EPC*15*n, reuses sTo after the Roe phase
   double* sE = reinterpret_cast<double*>(sQ + EPC * kNQ * n);  // EPC*n enstrophy
   for (int i = threadIdx.x; i < ne * kNS * n; i += NT) sU[i] = R::ld(U + e0 * kNS * n + i);
   for (int i = threadIdx.x; i < ne * 3 * kNS * nf; i += NT) {
@@ -218,9 +219,29 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
     int en = face_neighbour((int)e, 2 * l, ops.nx, ops.ny, ops.nz);
     sTp[i] = R::ld(Tu + (e * 6 + 2 * l + 1) * kNS * nf + r2);
     sTm[i] = R::ld(Tu + ((long)en * 6 + 2 * l + 1) * kNS * nf + r2);
+    sTo[i] = R::ld(Tu + (e * 6 + 2 * l) * kNS * nf + r2);
   }
-  if (threadIdx.x == 0) s_next = 0;
   __syncthreads();
+  // Roe flux on the three minus faces (numericalFluxC, solver.cpp:1194-1374):
+  // each face is computed once, here, by the element on its plus side; the
+  // element on the minus side uses its negation (the flux is antisymmetric).
+  for (int i = threadIdx.x; i < ne * 3 * nf; i += NT) {
+    const int es2 = i / (3 * nf);
+    const int r = i - es2 * 3 * nf;
+    const int l = r / nf, t = r - l * nf;
+    T uK[kNS], uN[kNS], F[kNS];
+#pragma unroll
+    for (int v = 0; v < kNS; ++v) {
+      uK[v] = sTo[((es2 * 3 + l) * kNS + v) * nf + t];
+      uN[v] = sTm[((es2 * 3 + l) * kNS + v) * nf + t];
+    }
+    if (l == 0) roe_flux<0>(uN, uK, false, o, F);
+    else if (l == 1) roe_flux<1>(uN, uK, false, o, F);
+    else roe_flux<2>(uN, uK, false, o, F);
+#pragma unroll
+    for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + v * nf + t, F[v]);
+  }
+  __syncthreads();  // the own -l traces are dead: Q takes their space
   const int es = threadIdx.x / n, q = threadIdx.x % n;
   if (es < ne) {
     const int c[3] = {q % N, (q / N) % N, q / (N * N)};
@@ -284,45 +305,20 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
       ens[e0 + threadIdx.x] = acc;
     }
   }
-  // One work list: the Roe flux on the three minus faces, then the
-  // minus-face traces of Q.
-  //  * Roe (numericalFluxC, solver.cpp:1194-1374): each face is computed
-  //    once, here, by the element on its plus side; the element on the minus
-  //    side uses its negation (the flux is antisymmetric).
-  //  * Tq[e][l][c][t] = sum_qn lm[qn] Q[e][c][pt(l,qn,t)].
-  const int nR = ne * 3 * nf;
-  for_each_item(&s_next, nR + ne * 3 * kNQ * nf, [&](int i) {
-    if (i < nR) {
-      const int es2 = i / (3 * nf);
-      const int r = i - es2 * 3 * nf;
-      const int l = r / nf, t = r - l * nf;
-      const auto* own = Tu + ((e0 + es2) * 6 + 2 * l) * kNS * nf + t;  // own -l traces
-      T uK[kNS], uN[kNS], F[kNS];
+  // minus-face traces of Q: Tq[e][l][c][t] = sum_qn lm[qn] Q[e][c][pt(l,qn,t)]
+  for (int i = threadIdx.x; i < ne * 3 * kNQ * nf; i += NT) {
+    int es2 = i / (3 * kNQ * nf);
+    int r = i - es2 * 3 * kNQ * nf;
+    int l = r / (kNQ * nf);
+    int r2 = r - l * kNQ * nf;
+    int cc = r2 / nf, t = r2 - cc * nf;
+    const int st = stride_of<N>(l);
+    const T* row = sQ + (es2 * kNQ + cc) * n + face_point<N>(l, 0, t);
+    Acc<T> acc;
 #pragma unroll
-      for (int v = 0; v < kNS; ++v) {
-        uK[v] = R::ld(own + v * nf);
-        uN[v] = sTm[((es2 * 3 + l) * kNS + v) * nf + t];
-      }
-      if (l == 0) roe_flux<0>(uN, uK, false, o, F);
-      else if (l == 1) roe_flux<1>(uN, uK, false, o, F);
-      else roe_flux<2>(uN, uK, false, o, F);
-#pragma unroll
-      for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + v * nf + t, F[v]);
-    } else {
-      const int j = i - nR;
-      const int es2 = j / (3 * kNQ * nf);
-      const int r = j - es2 * 3 * kNQ * nf;
-      const int l = r / (kNQ * nf);
-      const int r2 = r - l * kNQ * nf;
-      const int cc = r2 / nf, t = r2 - cc * nf;
-      const int st = stride_of<N>(l);
-      const T* row = sQ + (es2 * kNQ + cc) * n + face_point<N>(l, 0, t);
-      Acc<T> acc;
-#pragma unroll
-      for (int qn = 0; qn < N; ++qn) acc.add(o.lm[qn], row[qn * st]);
-      R::st(Tq + (e0 + es2) * 3 * kNQ * nf + r, acc.get());
-    }
-  });
+    for (int qn = 0; qn < N; ++qn) acc.add(o.lm[qn], row[qn * st]);
+    R::st(Tq + (e0 + es2) * 3 * kNQ * nf + r, acc.get());
+  }
 }
 
 template <int N, class T>
@@ -488,50 +484,63 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
   T* sF = reinterpret_cast<T*>(smem_raw);  // EPC*15*n   volume flux Fc - Fv
   T* sFs = sF + EPC * kNQ * n;             // EPC*6*5*nf face flux sums
   T* sU = sF;                              // EPC*5*n, aliases sF after use
-  __shared__ int s_next;                   // the work list's counter
   const int es = threadIdx.x / n, q = threadIdx.x % n;
   const bool act = es < ne;
   const int c[3] = {q % N, (q / N) % N, q / (N * N)};
-  if (threadIdx.x == 0) s_next = 0;
-  __syncthreads();
-  // 1-2. One work list: the volume fluxes at the Gauss points (the heavier
-  // items, first), then the numerical fluxes at the face points.
+  // 1-2. The volume fluxes at the Gauss points and the numerical fluxes at
+  // the face points (ne*6*nf of them, more than there are threads).
   const int nV = ne * n;
-  for_each_item(&s_next, nV + ne * 6 * nf, [&](int i) {
-    if (i < nV) {
-      const int es2 = i / n, q2 = i - es2 * n;
-      const long e = e0 + es2;
-      T u[kNS], Du[kNQ];
+  auto volume_item = [&](int i) {
+    const int es2 = i / n, q2 = i - es2 * n;
+    const long e = e0 + es2;
+    T u[kNS], Du[kNQ];
 #pragma unroll
-      for (int v = 0; v < kNS; ++v) u[v] = R::ld(a.Us + (e * kNS + v) * n + q2);
+    for (int v = 0; v < kNS; ++v) u[v] = R::ld(a.Us + (e * kNS + v) * n + q2);
 #pragma unroll
-      for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(a.Q + (e * kNQ + k) * n + q2);
-      Euler<T> es_ = euler_state(u, o);
-      ViscPre<T> P;
-      visc_pre(u, Du, P);
+    for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(a.Q + (e * kNQ + k) * n + q2);
+    Euler<T> es_ = euler_state(u, o);
+    ViscPre<T> P;
+    visc_pre(u, Du, P);
 #pragma unroll
-      for (int l = 0; l < 3; ++l) {
-        T F[kNS];
-        euler_column(u, es_, l, F);
-        if (l == 0) sub_visc_column<0>(P, o, F);
-        else if (l == 1) sub_visc_column<1>(P, o, F);
-        else sub_visc_column<2>(P, o, F);
+    for (int l = 0; l < 3; ++l) {
+      T F[kNS];
+      euler_column(u, es_, l, F);
+      if (l == 0) sub_visc_column<0>(P, o, F);
+      else if (l == 1) sub_visc_column<1>(P, o, F);
+      else sub_visc_column<2>(P, o, F);
 #pragma unroll
-        for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + l * kNS + v) * n + q2] = F[v];
-      }
-    } else {
-      const int j = i - nV;
-      const int fes = j / (6 * nf);
-      const int r = j - fes * 6 * nf;
-      const int f = r / nf, t = r - f * nf;
-      T* out = sFs + (fes * 6 + f) * kNS * nf + t;
-      switch (f >> 1) {
-        case 0: face_flux<N, 0>(a, ops, o, e0 + fes, f, t, out); break;
-        case 1: face_flux<N, 1>(a, ops, o, e0 + fes, f, t, out); break;
-        default: face_flux<N, 2>(a, ops, o, e0 + fes, f, t, out); break;
-      }
+      for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + l * kNS + v) * n + q2] = F[v];
     }
-  });
+  };
+  auto face_item = [&](int j) {
+    const int fes = j / (6 * nf);
+    const int r = j - fes * 6 * nf;
+    const int f = r / nf, t = r - f * nf;
+    T* out = sFs + (fes * 6 + f) * kNS * nf + t;
+    switch (f >> 1) {
+      case 0: face_flux<N, 0>(a, ops, o, e0 + fes, f, t, out); break;
+      case 1: face_flux<N, 1>(a, ops, o, e0 + fes, f, t, out); break;
+      default: face_flux<N, 2>(a, ops, o, e0 + fes, f, t, out); break;
+    }
+  };
+  if constexpr (std::is_same<T, dd>::value) {
+    // The FP32-pair path is latency-bound: one work list over both kinds
+    // (volume items, the heavier, first) keeps every warp busy.  Measured
+    // at 64^3 p=4: 8.31 -> 8.12 ms per launch.
+    __shared__ int s_next;  // the work list's counter
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    for_each_item(&s_next, nV + ne * 6 * nf, [&](int i) {
+      if (i < nV) volume_item(i);
+      else face_item(i - nV);
+    });
+  } else {
+    // The FP64 path is FP64-pipe bound and gains nothing from the list
+    // (measured 22.34 -> 22.47 ms): one volume item per thread, then the
+    // face items round-robin.
+    if (act) volume_item(threadIdx.x);
+    for (int j = threadIdx.x; j < ne * 6 * nf; j += Cfg<N, E>::T) face_item(j);
+  }
   __syncthreads();
   // 3. contraction: K at this Gauss point
   T K[kNS];
