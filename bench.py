@@ -459,11 +459,21 @@ def run_ours(args):
     if pg:
         pg.barrier()
     t0 = time.perf_counter()
+    its, calls = [], {"set_state": 0.0, "step": 0.0, "get_state": 0.0}
     for _ in range(Ke):
+        ti = time.perf_counter()
         s.set_state(host)
+        t1 = time.perf_counter()
         s.step(1)
+        t2 = time.perf_counter()
         s.get_state(host)
+        t3 = time.perf_counter()
+        its.append(t3 - ti)
+        calls["set_state"] += t1 - ti
+        calls["step"] += t2 - t1
+        calls["get_state"] += t3 - t2
     e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
+    its.sort()
     assert np.all(np.isfinite(host))
     # where an end-to-end step goes (untimed diagnostic: each call waited
     # for), with the transfers overlapped with the transforms in 8 chunks
@@ -488,7 +498,10 @@ def run_ours(args):
     s.set_transfer_chunks(8)
     e2e = {"value": ws * n_per_step * Ke / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes, "steps": Ke,
-           "ms_per_step": e2e_s * 1e3 / Ke, "breakdown_ms": breakdown}
+           "ms_per_step": e2e_s * 1e3 / Ke,
+           "iteration_ms": {"min": its[0] * 1e3, "median": its[len(its) // 2] * 1e3, "max": its[-1] * 1e3},
+           "call_ms": {k: v * 1e3 / Ke for k, v in calls.items()},
+           "breakdown_ms": breakdown}
 
     # ---- roofline of the dominant kernel (live event timings above)
     hbm_peak, peak_kind = read_peaks()
