@@ -158,12 +158,18 @@ def series_64(threads: int = 8, ref_dir: str | None = None, oracle_npz: str | No
         z = np.load(oracle_npz)
     assert abs(float(z["dt"]) - m["dt"]) <= 1e-15 * m["dt"]
     ens = dict(zip(z["enst_steps"].tolist(), z["enst"].tolist()))
-    for k in range(1, R + 1):  # the pin: every step of the reference window
+    # The pin: every step of the reference window.  The state samples and
+    # the KE at 1e-12.  The per-variable norms at 1e-11: the reference's
+    # driver sums the 32.8M squares of a variable in plain order, whose
+    # rounding (~sqrt(N) u ~ 6e-13 of the sum, up to ~1e-12 seen) exceeds
+    # the states' own difference; numpy sums pairwise.
+    NORM_TOL_REF = 1e-11
+    for k in range(1, R + 1):
         tot = np.sqrt(np.sum(ref_norms[k - 1]))
         e_ke = abs(z["ke"][k - 1] - ref_ke[k - 1]) / ref_ke[k - 1]
         e_s = np.linalg.norm(z["samples"][k - 1] - ref_samples[k - 1]) / np.linalg.norm(ref_samples[k - 1])
         e_n = np.max(np.abs(np.sqrt(z["norms"][k - 1]) - np.sqrt(ref_norms[k - 1]))) / tot
-        assert e_ke <= 1e-12 and e_s <= 1e-12 and e_n <= 1e-12, (k, e_ke, e_s, e_n)
+        assert e_ke <= 1e-12 and e_s <= 1e-12 and e_n <= NORM_TOL_REF, (k, e_ke, e_s, e_n)
     for k, v in ref_e:
         assert abs(ens[int(k)] - v) <= 1e-12 * abs(v), (k, ens[int(k)], v)
     keep = np.searchsorted(ref_idx, idx)
