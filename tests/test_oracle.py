@@ -178,3 +178,24 @@ def test_factored_enstrophy_equals_dense():
     b.set_factored(True)
     ea, eb = a.enstrophy(z["u0"]), b.enstrophy(z["u0"])
     assert abs(ea - eb) <= 1e-12 * abs(ea)
+
+
+def test_series_64_fixture_is_pinned_to_the_reference_window():
+    """tests/golden/series_n64_p4.npz holds the reference's own first 20
+    steps at 64^3 p=4 beside the factored oracle's 200: on the common steps
+    and entries they agree (samples and KE at 1e-12; the enstrophy of step
+    20 at 1e-12)."""
+    z = load("series_n64_p4.npz")
+    R = int(z["ref_steps"])
+    assert int(z["steps"]) == 200 and R >= 20
+    pos = np.searchsorted(z["ref_idx"], z["idx"])
+    assert np.array_equal(z["ref_idx"][pos], z["idx"])
+    for k in range(R):
+        assert abs(z["ke"][k] - z["ref_ke"][k]) <= 1e-12 * z["ref_ke"][k]
+        assert rel_l2(z["samples"][k], z["ref_samples"][k][pos]) <= 1e-12
+    ens = dict(zip(z["enst_steps"].tolist(), z["enst"].tolist()))
+    ref = dict(zip(z["ref_enst_steps"].tolist(), z["ref_enst"].tolist()))
+    common = sorted(set(ens) & set(ref))
+    assert common
+    for k in common:
+        assert abs(ens[k] - ref[k]) <= 1e-12 * abs(ref[k])
