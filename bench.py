@@ -335,7 +335,7 @@ def ensemble_variant(count, K, W, dev):
 
 
 CLOSURE_RECORDS = [os.path.join(ROOT, "local-dg_gb300", "examples", f)
-                   for f in ("closure_c5_result.json", "closure_c5_loop_result.json")]
+                   for f in ("closure_c5_result.json", "closure_c5_loop_result.json", "closure_c5_loop2_result.json")]
 
 
 def learned_variant(K, W, dev):
@@ -345,8 +345,9 @@ def learned_variant(K, W, dev):
     network is trained briefly here on samples from a 32^3 p=4 state, which
     is enough to time its inference; the accuracy of a fully trained closure
     comes from the committed records of the closure study
-    (closure_c5_result.json, closure_c5_loop_result.json, made by
-    examples/closure_tgv.py); the best of their variants is reported."""
+    (closure_c5_result.json, closure_c5_loop_result.json,
+    closure_c5_loop2_result.json, made by examples/closure_tgv.py); the best
+    of their variants is reported."""
     import torch
     import ldg
     out = {"coarse": "16^3 p=2 FP64, CFL 0.01", "network": "540-128-128-135 GELU, BF16 mma.sync"}
