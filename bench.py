@@ -459,6 +459,12 @@ def run_ours(args):
     Ke = 10
     if pg:
         pg.barrier()
+    # The interpreter's cyclic garbage collector stays off in the timed loop
+    # (as timeit keeps it off): its occasional full passes over the
+    # interpreter's objects took tens of ms inside single iterations.
+    import gc
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     its, calls = [], {"set_state": 0.0, "step": 0.0, "get_state": 0.0}
     for _ in range(Ke):
@@ -473,7 +479,9 @@ def run_ours(args):
         calls["set_state"] += t1 - ti
         calls["step"] += t2 - t1
         calls["get_state"] += t3 - t2
-    e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
+    e2e_elapsed = time.perf_counter() - t0
+    gc.enable()
+    e2e_s = max_over_ranks(e2e_elapsed, pg)
     its.sort()
     assert np.all(np.isfinite(host))
     # where an end-to-end step goes (untimed diagnostic: each call waited
