@@ -125,6 +125,17 @@ int ldg_get_state(ldg_solver* s, double* u, int where);
  * one range overlaps the basis transform of the previous one; 1 copies the
  * whole state before transforming it.  (No reference counterpart.) */
 int ldg_set_transfer_chunks(ldg_solver* s, int chunks);
+/* ldg_set_state(u_in) + ldg_step(nsteps) + ldg_get_state(u_out) with host
+ * buffers, bit for bit, in one call that overlaps the transfers with the
+ * step: the upload comes in z-plane chunks and stage 0's gradient pass of a
+ * chunk starts as soon as the chunk and its -z neighbour plane are there;
+ * the last stage's RHS pass runs chunk by chunk and each chunk of the new
+ * state goes back to the host while the next one is computed.  For a
+ * caller that keeps the state on the host, as the reference keeps
+ * Solver::u (solver.h:44) around dgTimeStep (solver.cpp:295-453).  u_in
+ * may equal u_out.  Returns once u_out holds the result.  With a closure
+ * attached it runs the three calls in sequence. */
+int ldg_advance_host(ldg_solver* s, const double* u_in, double* u_out, int nsteps);
 
 /* Resets the state to the Taylor-Green vortex (solver.cpp:194-236) and the
  * step counter to 0. */

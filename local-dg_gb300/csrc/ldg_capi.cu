@@ -276,14 +276,16 @@ cudaError_t launch_traces(const double* U, void* Ucopy, void* Tu, int nE, const 
 }
 template <int N, class T>
 cudaError_t launch_grad(const void* U, const void* Tu, void* Q, void* Tq, void* Fm, double* ens,
-                        const DevOps& ops, const OpsT<T>& o, cudaStream_t st) {
+                        const DevOps& ops, const OpsT<T>& o, cudaStream_t st, int ebase = 0, int eend = -1) {
   using S = typename Real<T>::S;
-  k_grad<N, T><<<grid_for<N>(ops.nE), Cfg<N>::T, smem_grad<N>(), st>>>((const S*)U, (const S*)Tu, (S*)Q,
-                                                                        (S*)Tq, (S*)Fm, ens, ops, o);
+  if (eend < 0) eend = ops.nE;
+  k_grad<N, T><<<grid_for<N>(eend - ebase), Cfg<N>::T, smem_grad<N>(), st>>>(
+      (const S*)U, (const S*)Tu, (S*)Q, (S*)Tq, (S*)Fm, ens, ops, o, ebase, eend);
   return cudaGetLastError();
 }
 template <int N, class T>
-cudaError_t launch_rhs(const StageCall& c, const DevOps& ops, const OpsT<T>& o, cudaStream_t st) {
+cudaError_t launch_rhs(const StageCall& c, const DevOps& ops, const OpsT<T>& o, cudaStream_t st, int ebase = 0,
+                       int eend = -1) {
   using S = typename Real<T>::S;
   StageArgs<T> a{};
   a.Us = (const S*)c.Us;
@@ -302,7 +304,8 @@ cudaError_t launch_rhs(const StageCall& c, const DevOps& ops, const OpsT<T>& o, 
   a.cacc = c.cacc;
   a.cnext = c.cnext;
   a.stage = c.stage;
-  k_rhs<N, T><<<grid_for<N>(ops.nE), Cfg<N>::T, smem_rhs<N>(), st>>>(a, ops, o);
+  if (eend < 0) eend = ops.nE;
+  k_rhs<N, T><<<grid_for<N>(eend - ebase), Cfg<N>::T, smem_rhs<N>(), st>>>(a, ops, o, ebase, eend);
   return cudaGetLastError();
 }
 
@@ -432,13 +435,17 @@ cudaError_t s_traces(ldg_solver* s, bool mixed, const double* U, void* Ucopy, vo
   if (mixed) LDG_DISPATCH(s->N, (launch_traces<NN, dd>(U, Ucopy, Tu, s->nE, s->odd, s->stream)));
   LDG_DISPATCH(s->N, (launch_traces<NN, double>(U, Ucopy, Tu, s->nE, s->o64, s->stream)));
 }
-cudaError_t s_grad(ldg_solver* s, bool mixed, const void* U, const void* Tu, double* ens) {
-  if (mixed) LDG_DISPATCH(s->N, (launch_grad<NN, dd>(U, Tu, s->Q, s->Tq, s->Fm, ens, s->ops, s->odd, s->stream)));
-  LDG_DISPATCH(s->N, (launch_grad<NN, double>(U, Tu, s->Q, s->Tq, s->Fm, ens, s->ops, s->o64, s->stream)));
+// Elements [ebase, eend) (eend < 0: all).
+cudaError_t s_grad(ldg_solver* s, bool mixed, const void* U, const void* Tu, double* ens, int ebase = 0,
+                   int eend = -1) {
+  if (mixed)
+    LDG_DISPATCH(s->N, (launch_grad<NN, dd>(U, Tu, s->Q, s->Tq, s->Fm, ens, s->ops, s->odd, s->stream, ebase, eend)));
+  LDG_DISPATCH(s->N,
+               (launch_grad<NN, double>(U, Tu, s->Q, s->Tq, s->Fm, ens, s->ops, s->o64, s->stream, ebase, eend)));
 }
-cudaError_t s_rhs(ldg_solver* s, bool mixed, const StageCall& c) {
-  if (mixed) LDG_DISPATCH(s->N, (launch_rhs<NN, dd>(c, s->ops, s->odd, s->stream)));
-  LDG_DISPATCH(s->N, (launch_rhs<NN, double>(c, s->ops, s->o64, s->stream)));
+cudaError_t s_rhs(ldg_solver* s, bool mixed, const StageCall& c, int ebase = 0, int eend = -1) {
+  if (mixed) LDG_DISPATCH(s->N, (launch_rhs<NN, dd>(c, s->ops, s->odd, s->stream, ebase, eend)));
+  LDG_DISPATCH(s->N, (launch_rhs<NN, double>(c, s->ops, s->o64, s->stream, ebase, eend)));
 }
 
 // nodal (reference layout, in s->nodal) -> Un and the traces of Un; on the
@@ -1065,15 +1072,28 @@ int ldg_rhs(ldg_solver* s, const double* u_curr, double* k, int where) {
   return LDG_OK;
 }
 
-int ldg_step(ldg_solver* s, int nsteps) {
-  if (!s) return fail(LDG_ERR_INVALID, "null solver");
-  if (nsteps < 0) return fail(LDG_ERR_INVALID, "negative step count");
-  if (nsteps == 0) return LDG_OK;
-  LDG_CUDA(cudaSetDevice(s->cfg.device));
-  int st = ensure_ke_capacity(s, s->step + nsteps + 1);
-  if (st) return st;
-  if (s->cfg.check_finite) LDG_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
+}  // extern "C"
+
+namespace {
+
+// Plane-aligned chunk c of `chunks` over the elements: whole z-planes
+// [nz c / chunks, nz (c+1) / chunks), so that an element's -z neighbour
+// lies in its own chunk or the one before (except plane 0's, in the last).
+void plane_chunk(const ldg_solver* s, int chunks, int c, int* e0, int* e1) {
+  const long P = (long)s->cfg.nx * s->cfg.ny;
+  *e0 = (int)(P * ((long)s->cfg.nz * c / chunks));
+  *e1 = (int)(P * ((long)s->cfg.nz * (c + 1) / chunks));
+}
+
+// The RK4 steps of ldg_step.  first_grad_done: stage 0's gradient pass of
+// the first step has run already (ldg_advance_host overlaps it with the
+// upload).  u_out (host): the last stage's RHS pass runs in plane chunks and
+// each chunk's new state is transformed and copied out on the copy stream
+// as soon as it is written; the caller synchronises the copy stream.
+int step_loop(ldg_solver* s, int nsteps, bool first_grad_done, double* u_out) {
   const bool mixed = s->mixed;
+  const long per = (long)kNS * s->n;
+  const int chunks = std::max(1, std::min(s->xfer_chunks, s->cfg.nz));
   for (int it = 0; it < nsteps; ++it) {
     const int cur = s->cur;
     for (int stage = 0; stage < 4; ++stage) {
@@ -1082,9 +1102,11 @@ int ldg_step(ldg_solver* s, int nsteps) {
       const void* Uin = (stage == 0 && !mixed) ? (const void*)s->Un : (const void*)s->Us;
       double* Tu_in = s->Tu[(stage & 1) ? 1 - cur : cur];
       double* Tu_out = s->Tu[(stage & 1) ? cur : 1 - cur];
-      LDG_CUDA(tic(s, 0));
-      LDG_CUDA(s_grad(s, mixed, Uin, Tu_in, nullptr));
-      LDG_CUDA(toc(s));
+      if (!(first_grad_done && it == 0 && stage == 0)) {
+        LDG_CUDA(tic(s, 0));
+        LDG_CUDA(s_grad(s, mixed, Uin, Tu_in, nullptr));
+        LDG_CUDA(toc(s));
+      }
       if (s->closure) {
         int cst = closure_correction(s->closure, solver_view(s), (const double*)Uin, s->Q, s->Kadd, s->stream);
         if (cst) return cst;
@@ -1105,9 +1127,26 @@ int ldg_step(ldg_solver* s, int nsteps) {
       c.cacc = s->dt * kRkB[stage];
       c.cnext = stage < 3 ? s->dt * kRkA[stage] : 0.0;
       c.stage = stage;
-      LDG_CUDA(tic(s, 1));
-      LDG_CUDA(s_rhs(s, mixed, c));
-      LDG_CUDA(toc(s));
+      if (u_out && it == nsteps - 1 && stage == 3) {
+        for (int k = 0; k < chunks; ++k) {
+          int e0, e1;
+          plane_chunk(s, chunks, k, &e0, &e1);
+          if (e1 == e0) continue;
+          LDG_CUDA(tic(s, 1));
+          LDG_CUDA(s_rhs(s, mixed, c, e0, e1));
+          LDG_CUDA(toc(s));
+          // the chunk's new state (Uacc) in the reference layout, to the host
+          LDG_CUDA(d_transform(s->N, s->Uacc + e0 * per, s->nodal + e0 * per, e1 - e0, s->ops, 1, s->stream));
+          LDG_CUDA(cudaEventRecord(s->xev[k], s->stream));
+          LDG_CUDA(cudaStreamWaitEvent(s->xfer, s->xev[k], 0));
+          LDG_CUDA(cudaMemcpyAsync(u_out + e0 * per, s->nodal + e0 * per, (size_t)(e1 - e0) * per * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s->xfer));
+        }
+      } else {
+        LDG_CUDA(tic(s, 1));
+        LDG_CUDA(s_rhs(s, mixed, c));
+        LDG_CUDA(toc(s));
+      }
     }
     // After four stages Tu[cur] holds the traces of Uacc = u^{n+1}.
     std::swap(s->Un, s->Uacc);
@@ -1119,13 +1158,84 @@ int ldg_step(ldg_solver* s, int nsteps) {
     s->step += 1;
     if (s->timing && s->ev_used > 4096) LDG_CUDA(harvest_times(s));
   }
-  if (s->cfg.check_finite) {
-    int h = 0;
-    LDG_CUDA(cudaMemcpyAsync(&h, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    LDG_CUDA(cudaStreamSynchronize(s->stream));
-    if (h) return fail(LDG_ERR_NONFINITE, "non-finite value in the state");
-  }
   return LDG_OK;
+}
+
+int check_finite_flag(ldg_solver* s) {
+  if (!s->cfg.check_finite) return LDG_OK;
+  int h = 0;
+  LDG_CUDA(cudaMemcpyAsync(&h, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  LDG_CUDA(cudaStreamSynchronize(s->stream));
+  if (h) return fail(LDG_ERR_NONFINITE, "non-finite value in the state");
+  return LDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ldg_step(ldg_solver* s, int nsteps) {
+  if (!s) return fail(LDG_ERR_INVALID, "null solver");
+  if (nsteps < 0) return fail(LDG_ERR_INVALID, "negative step count");
+  if (nsteps == 0) return LDG_OK;
+  LDG_CUDA(cudaSetDevice(s->cfg.device));
+  int st = ensure_ke_capacity(s, s->step + nsteps + 1);
+  if (st) return st;
+  if (s->cfg.check_finite) LDG_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
+  if ((st = step_loop(s, nsteps, false, nullptr))) return st;
+  return check_finite_flag(s);
+}
+
+int ldg_advance_host(ldg_solver* s, const double* u_in, double* u_out, int nsteps) {
+  if (!s || !u_in || !u_out) return fail(LDG_ERR_INVALID, "ldg_advance_host: null argument");
+  if (nsteps < 1) return fail(LDG_ERR_INVALID, "ldg_advance_host: nsteps must be at least 1");
+  LDG_CUDA(cudaSetDevice(s->cfg.device));
+  int st;
+  if (s->closure) {  // the closure needs the whole gradient before any RHS: the plain sequence
+    if ((st = ldg_set_state(s, u_in, LDG_HOST)) || (st = ldg_step(s, nsteps))) return st;
+    return ldg_get_state(s, u_out, LDG_HOST);
+  }
+  if ((st = ensure_ke_capacity(s, s->step + nsteps + 1)) || (st = ensure_xfer(s))) return st;
+  if (s->cfg.check_finite) LDG_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
+  const bool mixed = s->mixed;
+  const long per = (long)kNS * s->n;
+  const int chunks = std::max(1, std::min(s->xfer_chunks, s->cfg.nz));
+  const void* Uin0 = mixed ? (const void*)s->Us : (const void*)s->Un;
+  double* Tu0 = s->Tu[s->cur];
+  // 1. Upload in plane chunks: copy (copy stream), transform and traces
+  //    (solver stream).  Stage 0's gradient pass of chunk c needs the traces
+  //    of its -z neighbours, which lie in chunks c-1 and c, so it follows
+  //    chunk c's upload; chunk 0's neighbours across the periodic wrap
+  //    arrive with the last chunk, so its gradient pass goes last.
+  LDG_CUDA(cudaEventRecord(s->xev[kMaxXferChunks], s->stream));
+  LDG_CUDA(cudaStreamWaitEvent(s->xfer, s->xev[kMaxXferChunks], 0));
+  for (int c = 0; c < chunks; ++c) {
+    int e0, e1;
+    plane_chunk(s, chunks, c, &e0, &e1);
+    if (e1 == e0) continue;
+    LDG_CUDA(cudaMemcpyAsync(s->nodal + e0 * per, u_in + e0 * per, (size_t)(e1 - e0) * per * sizeof(double),
+                             cudaMemcpyHostToDevice, s->xfer));
+    LDG_CUDA(cudaEventRecord(s->xev[c], s->xfer));
+    LDG_CUDA(cudaStreamWaitEvent(s->stream, s->xev[c], 0));
+    LDG_CUDA(d_transform(s->N, s->nodal + e0 * per, s->Un + e0 * per, e1 - e0, s->ops, 0, s->stream));
+    LDG_CUDA(s_traces_range(s, mixed, s->Un, mixed ? (void*)s->Us : nullptr, Tu0, e0, e1 - e0));
+    if (c > 0) {
+      LDG_CUDA(tic(s, 0));
+      LDG_CUDA(s_grad(s, mixed, Uin0, Tu0, nullptr, e0, e1));
+      LDG_CUDA(toc(s));
+    }
+  }
+  {
+    int e0, e1;
+    plane_chunk(s, chunks, 0, &e0, &e1);
+    LDG_CUDA(tic(s, 0));
+    LDG_CUDA(s_grad(s, mixed, Uin0, Tu0, nullptr, e0, e1));
+    LDG_CUDA(toc(s));
+  }
+  // 2. The steps; the last stage's RHS pass feeds the download chunk by chunk.
+  if ((st = step_loop(s, nsteps, true, u_out))) return st;
+  LDG_CUDA(cudaStreamSynchronize(s->xfer));
+  return check_finite_flag(s);
 }
 
 int ldg_time_step(ldg_solver* s) {

@@ -329,10 +329,11 @@ __global__ void __launch_bounds__(Cfg<N>::T, Cfg<N>::T == 256 ? 4 : 1) k_grad(co
                                                     typename Real<T>::S* __restrict__ Fm,
                                                     double* __restrict__ ens,
                                                     const __grid_constant__ DevOps ops,
-                                                    const __grid_constant__ OpsT<T> o) {
+                                                    const __grid_constant__ OpsT<T> o, int ebase, int eend) {
+  // elements [ebase, eend), EPC per CTA
   extern __shared__ double smem_raw[];
-  const long e0 = (long)blockIdx.x * Cfg<N>::EPC;
-  const int ne = (int)min((long)Cfg<N>::EPC, ops.nE - e0);
+  const long e0 = ebase + (long)blockIdx.x * Cfg<N>::EPC;
+  const int ne = (int)min((long)Cfg<N>::EPC, eend - e0);
   grad_body<N, T>(U, Tu, Q, Tq, Fm, ens, ops, o, e0, ne, smem_raw);
 }
 
@@ -613,10 +614,11 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
 template <int N, class T>
 __global__ void __launch_bounds__(Cfg<N>::T, Cfg<N>::T == 256 ? 4 : 1) k_rhs(const __grid_constant__ StageArgs<T> a,
                                                    const __grid_constant__ DevOps ops,
-                                                   const __grid_constant__ OpsT<T> o) {
+                                                   const __grid_constant__ OpsT<T> o, int ebase, int eend) {
+  // elements [ebase, eend), EPC per CTA
   extern __shared__ double smem_raw[];
-  const long e0 = (long)blockIdx.x * Cfg<N>::EPC;
-  const int ne = (int)min((long)Cfg<N>::EPC, ops.nE - e0);
+  const long e0 = ebase + (long)blockIdx.x * Cfg<N>::EPC;
+  const int ne = (int)min((long)Cfg<N>::EPC, eend - e0);
   rhs_body<N, T>(a, ops, o, e0, ne, smem_raw);
 }
 

@@ -88,7 +88,7 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   const int grid = (nE + C::EPC - 1) / C::EPC;
   k_transform<N><<<grid, C::T, sm_tr, st>>>(u, U, nE, kNS, ops, 0);
   k_traces<N, double><<<grid, C::T, sm_trc, st>>>(U, nullptr, Tu, nE, o);
-  k_grad<N, double><<<grid, C::T, sm_g, st>>>(U, Tu, Q, Tq, Fm, nullptr, ops, o);
+  k_grad<N, double><<<grid, C::T, sm_g, st>>>(U, Tu, Q, Tq, Fm, nullptr, ops, o, 0, ops.nE);
   StageArgs<double> a{};
   std::memset(&a, 0, sizeof(a));
   a.Us = U;
@@ -98,7 +98,7 @@ cudaError_t run_rhs(const double* u, double* k, double* scratch, const DevOps& o
   a.Fm = Fm;
   a.Kout = U;  // each thread overwrites only the Gauss point it alone read
   a.stage = -1;
-  k_rhs<N, double><<<grid, C::T, sm_r, st>>>(a, ops, o);
+  k_rhs<N, double><<<grid, C::T, sm_r, st>>>(a, ops, o, 0, ops.nE);
   k_transform<N><<<grid, C::T, sm_tr, st>>>(U, k, nE, kNS, ops, 1);
   return cudaGetLastError();
 }

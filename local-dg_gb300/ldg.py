@@ -147,6 +147,7 @@ SIGNATURES = {
     "ldg_probe_fp64": (_i, [_i, _dp, _dp, _dp]),
     "ldg_probe_contraction": (_i, [_vp, _i, _i, _dp, _dp]),
     "ldg_set_transfer_chunks": (_i, [_vp, _i]),
+    "ldg_advance_host": (_i, [_vp, _vp, _vp, _i]),
     "ldg_rhs_noalloc": (_i, [ctypes.POINTER(LdgConfig), _vp, _vp, _vp]),
     "ldg_ensemble_create": (_i, [ctypes.POINTER(LdgConfig), _i, ctypes.POINTER(_vp)]),
     "ldg_ensemble_destroy": (_i, [_vp]),
@@ -343,6 +344,16 @@ class Solver:
         """Host transfers in `chunks` element ranges overlapped with the basis
         transforms (1: copy everything, then transform)."""
         _check(load().ldg_set_transfer_chunks(self._h, chunks), "ldg_set_transfer_chunks")
+
+    def advance_host(self, u_in, u_out, nsteps: int = 1) -> None:
+        """set_state(u_in), step(nsteps), get_state(u_out) in one call that
+        overlaps the host transfers with the step (host numpy arrays; they
+        may be the same array)."""
+        a, _, ka = _arg(u_in)
+        b, _, kb = _arg(u_out)
+        assert isinstance(u_out, np.ndarray) and kb is u_out, "u_out must be a C-contiguous float64 array"
+        _check(load().ldg_advance_host(self._h, a, b, nsteps), "ldg_advance_host")
+        del ka, kb
 
     def get_state(self, out=None):
         if out is None:

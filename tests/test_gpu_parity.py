@@ -222,3 +222,35 @@ def test_transfer_chunking_changes_no_bit():
     with pytest.raises(ldg.LdgError):
         with ldg.Solver(2, 3) as s:
             s.set_transfer_chunks(0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_advance_host_equals_set_step_get(precision):
+    """ldg_advance_host overlaps the transfers with the first and last
+    passes of the steps; it must give the bits of ldg_set_state +
+    ldg_step + ldg_get_state, including the KE series, for several chunk
+    counts (z-plane chunks; 7 planes of 4 x 5 elements here) and in place."""
+    rng = np.random.default_rng(7)
+    with ldg.Solver(3, 4, 5, 7, steps=6, precision=precision) as s:
+        u0 = s.get_state()
+    u0[:, 1:4] += 0.01 * rng.standard_normal(u0[:, 1:4].shape)
+    for chunks in (1, 3, 8):
+        with ldg.Solver(3, 4, 5, 7, steps=6, precision=precision) as s:
+            s.set_transfer_chunks(chunks)
+            s.set_state(u0)
+            s.step(3)
+            want = s.get_state()
+            ke_want = s.ke_history()
+            s.set_state(want)  # the fused call below also restarts from the host copy
+            s.step(1)
+            want2 = s.get_state()
+        with ldg.Solver(3, 4, 5, 7, steps=6, precision=precision) as s:
+            s.set_transfer_chunks(chunks)
+            out = np.empty_like(u0)
+            s.advance_host(u0, out, 3)
+            assert np.array_equal(out, want), chunks
+            assert np.array_equal(s.ke_history(), ke_want), chunks
+            buf = out.copy()
+            s.advance_host(buf, buf, 1)  # in place
+            assert np.array_equal(buf, want2), chunks
