@@ -90,7 +90,8 @@ class _Fine:
 
 
 def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iters=10000, batch=4096, lr=1e-3,
-        hidden=128, amp=1e-2, data="projected", fine_precision="mixed", variants=None, device=0, log=None):
+        hidden=128, amp=1e-2, data="projected", fine_precision="mixed", variants=None, device=0, log=None,
+        eval_seed=SEED_EVAL):
     """The experiment; returns the summary and the KE series.  Each variant
     may name its own data set ("data": projected | loop | both; default the
     `data` argument); every data set needed is collected from the same fine
@@ -104,7 +105,7 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
     res = {"config": {"coarse": f"{coarse_nx}^3 p={P_COARSE} FP64, CFL 0.01",
                       "fine": f"{fine_nx}^3 p={P_FINE} {fine_precision}, CFL {fine_cfl}",
                       "t_end": t_end, "sample_dt": sample_dt, "iters": iters, "data": kinds,
-                      "seeds": {"train": [[SEED_TRAIN, 0], [SEED_TRAIN, 1]], "eval": [SEED_EVAL, 0]}}}
+                      "seeds": {"train": [[SEED_TRAIN, 0], [SEED_TRAIN, 1]], "eval": [eval_seed, 0]}}}
     series = {}
     closures = {k: ldg.Closure(p=P_COARSE, hidden=hidden, seed=7, device=device) for k in kinds}
     theta0 = closures[kinds[0]].get_params()
@@ -150,7 +151,7 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
 
     # ---- evaluation run (seed disjoint from training): held-out samples + KE
     t0 = time.perf_counter()
-    ev = _Fine(fine_nx, fine_steps, fine_cfl, amp, SEED_EVAL, 0, fine_precision, fine_view)
+    ev = _Fine(fine_nx, fine_steps, fine_cfl, amp, eval_seed, 0, fine_precision, fine_view)
     for k in range(n_times):
         fv = ev.fp64()
         for c in closures.values():
@@ -173,7 +174,7 @@ def run(coarse_nx=16, fine_nx=32, t_end=20.0, sample_dt=0.5, fine_cfl=0.02, iter
 
     def coarse_run(name, closure):
         t0 = time.perf_counter()
-        with ldg.Solver(P_COARSE, coarse_nx, steps=nc_steps, perturb_amp=amp, seed=SEED_EVAL, instance=0,
+        with ldg.Solver(P_COARSE, coarse_nx, steps=nc_steps, perturb_amp=amp, seed=eval_seed, instance=0,
                         device=device) as s:
             if closure is not None:
                 s.attach_closure(closure)

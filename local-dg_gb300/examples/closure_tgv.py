@@ -49,6 +49,8 @@ def main():
     ap.add_argument("--fine-nx", type=int, default=32)
     ap.add_argument("--data", default="projected", choices=["projected", "loop", "both"])
     ap.add_argument("--fine-precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--eval-seed", type=int, default=closure_study.SEED_EVAL,
+                    help="seed of the evaluation run and of the coarse runs (never a training seed)")
     ap.add_argument("--variants", default=None,
                     help="JSON list of closure variants, or @file with one (e.g. @closure_c5_variants.json)")
     args = ap.parse_args()
@@ -66,7 +68,7 @@ def main():
         coarse_nx=args.coarse_nx, fine_nx=args.fine_nx, t_end=args.t_end, sample_dt=args.sample_dt,
         fine_cfl=args.fine_cfl, iters=args.iters, batch=args.batch, lr=args.lr, hidden=args.hidden, amp=args.amp,
         data=args.data, fine_precision=args.fine_precision,
-        variants=variants,
+        variants=variants, eval_seed=args.eval_seed,
         log=lambda *a: print(*a, file=sys.stderr, flush=True))
     res["command"] = " ".join(["python", "local-dg_gb300/examples/closure_tgv.py"] + sys.argv[1:])
     with open(args.out, "w") as f:
