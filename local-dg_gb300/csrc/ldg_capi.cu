@@ -430,6 +430,15 @@ __global__ void __launch_bounds__(256) k_fp64_chain(double* out, long long* cycl
   }
 }
 
+// The flux kernels' FP64 reciprocal and reciprocal square root on n
+// operands (ldg_probe_recip).
+__global__ void k_recip(const double* __restrict__ x, double* __restrict__ r, double* __restrict__ rs, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    r[i] = rcp(x[i]);
+    rs[i] = rsqrt_(x[i]);
+  }
+}
+
 // Stage kernels in the solver's arithmetic (mixed: FP32 pairs) or FP64.
 cudaError_t s_traces(ldg_solver* s, bool mixed, const double* U, void* Ucopy, void* Tu) {
   if (mixed) LDG_DISPATCH(s->N, (launch_traces<NN, dd>(U, Ucopy, Tu, s->nE, s->odd, s->stream)));
@@ -1415,6 +1424,30 @@ int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* s
 }
 
 int ldg_probe_fp64_peak(int device, double* tflops) { return ldg_probe_fp64(device, tflops, nullptr, nullptr); }
+
+int ldg_probe_recip(int device, const double* x, double* r, double* rs, long n) {
+  if (n < 0 || (n > 0 && (!x || !r || !rs))) return fail(LDG_ERR_INVALID, "null buffer");
+  if (n == 0) return LDG_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(LDG_ERR_NODEVICE, "no CUDA device");
+  }
+  LDG_CUDA(cudaSetDevice(device));
+  double* d = nullptr;
+  LDG_CUDA(cudaMalloc((void**)&d, 3 * sizeof(double) * n));
+  cudaError_t err = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) {
+    const long blocks = std::min<long>((n + 255) / 256, 152L * 16);
+    k_recip<<<(int)blocks, 256>>>(d, d + n, d + 2 * n, n);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = cudaMemcpy(r, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess) err = cudaMemcpy(rs, d + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (err != cudaSuccess) return fail(LDG_ERR_CUDA, cudaGetErrorString(err));
+  return LDG_OK;
+}
 
 }  // extern "C"
 

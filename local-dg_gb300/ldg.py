@@ -145,6 +145,7 @@ SIGNATURES = {
     "ldg_kernel_times": (_i, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _i, _i]),
     "ldg_probe_fp64_peak": (_i, [_i, _dp]),
     "ldg_probe_fp64": (_i, [_i, _dp, _dp, _dp]),
+    "ldg_probe_recip": (_i, [_i, _vp, _vp, _vp, ctypes.c_long]),
     "ldg_probe_contraction": (_i, [_vp, _i, _i, _dp, _dp]),
     "ldg_set_transfer_chunks": (_i, [_vp, _i]),
     "ldg_advance_host": (_i, [_vp, _vp, _vp, _i]),
@@ -219,6 +220,16 @@ def probe_fp64(device: int = 0) -> dict:
     t, r, m = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     _check(load().ldg_probe_fp64(device, ctypes.byref(t), ctypes.byref(r), ctypes.byref(m)), "ldg_probe_fp64")
     return {"tflops": t.value, "fma_per_sm_clk": r.value, "sm_mhz": m.value}
+
+
+def probe_recip(x, device: int = 0):
+    """The flux kernels' FP64 reciprocal and reciprocal square root applied
+    on the device to the float64 array x: returns (1/x, 1/sqrt(x))."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    r, rs = np.empty_like(x), np.empty_like(x)
+    _check(load().ldg_probe_recip(device, x.ctypes.data, r.ctypes.data, rs.ctypes.data, x.size),
+           "ldg_probe_recip")
+    return r, rs
 
 
 class LdgError(RuntimeError):
