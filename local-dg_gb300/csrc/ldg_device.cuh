@@ -221,9 +221,9 @@ struct ViscPre {
   T div;
 };
 
+// ir = 1/rho, when the caller has it already
 template <class T>
-__device__ __forceinline__ void visc_pre(const T u[kNS], const T* Du, ViscPre<T>& P) {
-  T ir = rcp(u[0]);
+__device__ __forceinline__ void visc_pre(const T u[kNS], const T ir, const T* Du, ViscPre<T>& P) {
   P.v[0] = u[1] * ir;
   P.v[1] = u[2] * ir;
   P.v[2] = u[3] * ir;
@@ -237,6 +237,11 @@ __device__ __forceinline__ void visc_pre(const T u[kNS], const T* Du, ViscPre<T>
               (P.v[0] * P.G[0][j] + P.v[1] * P.G[1][j] + P.v[2] * P.G[2][j]);
   }
   P.div = P.G[0][0] + P.G[1][1] + P.G[2][2];
+}
+
+template <class T>
+__device__ __forceinline__ void visc_pre(const T u[kNS], const T* Du, ViscPre<T>& P) {
+  visc_pre(u, rcp(u[0]), Du, P);
 }
 
 // Column j of the viscous flux (solver.cpp:1136-1187): Newtonian stress with

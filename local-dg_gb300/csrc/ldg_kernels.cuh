@@ -501,7 +501,7 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
     for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(a.Q + (e * kNQ + k) * n + q2);
     Euler<T> es_ = euler_state(u, o);
     ViscPre<T> P;
-    visc_pre(u, Du, P);
+    visc_pre(u, es_.ir, Du, P);
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
       T F[kNS];
