@@ -338,6 +338,9 @@ def ensemble_variant(count, K, W, dev):
 
 CLOSURE_RECORDS = [os.path.join(ROOT, "local-dg_gb300", "examples", f)
                    for f in ("closure_c5_result.json", "closure_c5_loop_result.json", "closure_c5_loop2_result.json")]
+# The best variants re-judged against a fine run from an evaluation seed
+# that neither training nor the choice of variant saw.
+CLOSURE_SEED_CHECK = os.path.join(ROOT, "local-dg_gb300", "examples", "closure_c5_seed3003_result.json")
 
 
 def learned_variant(K, W, dev):
@@ -347,9 +350,7 @@ def learned_variant(K, W, dev):
     network is trained briefly here on samples from a 32^3 p=4 state, which
     is enough to time its inference; the accuracy of a fully trained closure
     comes from the committed records of the closure study
-    (closure_c5_result.json, closure_c5_loop_result.json,
-    closure_c5_loop2_result.json, made by examples/closure_tgv.py); the best
-    of their variants is reported."""
+    (recorded_closure)."""
     import torch
     import ldg
     out = {"coarse": "16^3 p=2 FP64, CFL 0.01", "network": "540-128-128-135 GELU, BF16 mma.sync"}
@@ -377,6 +378,17 @@ def learned_variant(K, W, dev):
                 rates[name] = {"value": s.dofs * s.nE * 4 * K / (ms * 1e-3), "ms_per_step": ms / K}
         out.update(rates)
         out["closure_overhead"] = rates["closure"]["ms_per_step"] / rates["plain"]["ms_per_step"]
+    out["recorded_a_posteriori"] = recorded_closure()
+    return out
+
+
+def recorded_closure():
+    """The a-posteriori accuracy of the fully trained closure from the
+    committed records of the closure study: the best variant over the
+    records on the main evaluation seed, against plain LDG on that seed, and
+    the best variants re-judged on a second evaluation seed.  None if a
+    record is missing."""
+    rec_out = None
     try:
         keys = ("rms_err_rel", "max_err_rel", "final_ke", "peak_time")
         runs, cmds = {}, {}
@@ -390,7 +402,7 @@ def learned_variant(K, W, dev):
                     runs[k] = dict(v, source=src)
             cmds[src] = rec.get("command")
         best = min(runs, key=lambda k: runs[k]["rms_err_rel"])
-        out["recorded_a_posteriori"] = {
+        rec_out = {
             "sources": cmds, "config": rec.get("config"),
             "metric": "KE-dissipation-rate error (solver.cpp:438-440) vs the fine run, t >= 1, rel. to its peak",
             "fine": {k: ap["fine"].get(k) for k in ("final_ke", "peak_time")},
@@ -399,9 +411,19 @@ def learned_variant(K, W, dev):
                                  fallback_element_stages=runs[best].get("fallback_element_stages")),
             "closure_beats_plain": runs[best]["rms_err_rel"] < ap["plain"]["rms_err_rel"],
             "variants_tried": len(runs)}
+        with open(CLOSURE_SEED_CHECK) as f:
+            chk = json.load(f)
+        cap = chk["a_posteriori"]
+        closures = {k: {m: v.get(m) for m in keys} for k, v in cap.items() if k not in ("fine", "plain")}
+        rec_out["second_eval_seed"] = {
+            "source": os.path.relpath(CLOSURE_SEED_CHECK, ROOT), "command": chk.get("command"),
+            "eval_seed": chk["config"]["seeds"]["eval"][0],
+            "plain": {m: cap["plain"].get(m) for m in keys}, "closures": closures,
+            "closure_beats_plain": all(v["rms_err_rel"] < cap["plain"]["rms_err_rel"] and
+                                       v["max_err_rel"] < cap["plain"]["max_err_rel"] for v in closures.values())}
     except (OSError, KeyError, ValueError):
-        out["recorded_a_posteriori"] = None
-    return out
+        return None
+    return rec_out
 
 
 def contraction_probe(s, reps=5):

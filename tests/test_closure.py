@@ -215,3 +215,18 @@ def test_compare_measures_rms_and_max_after_the_transient():
     assert same["rms_err_rel"] < 1e-9 and same["max_err_rel"] < 1e-9
     off = cs.compare(ke_ref - 0.001 * t, dt, t_ref, e_ref, scale)  # +0.001 dissipation everywhere
     assert abs(off["rms_err_rel"] - 0.001 / scale) < 1e-9 and abs(off["max_err_rel"] - 0.001 / scale) < 1e-9
+
+
+def test_recorded_closure_beats_plain_on_two_evaluation_seeds():
+    """The committed closure-study records: the best variant beats plain
+    coarse LDG on the main evaluation seed, and the best variants, re-run
+    against a fine run from a seed that neither training nor the choice of
+    variant saw, beat it there too (rms and max dissipation-rate error)."""
+    import bench
+    r = bench.recorded_closure()
+    assert r is not None
+    assert r["closure_beats_plain"]
+    chk = r["second_eval_seed"]
+    assert chk["eval_seed"] != r["config"]["seeds"]["eval"][0]
+    assert chk["eval_seed"] not in [s for s, _ in r["config"]["seeds"]["train"]]
+    assert chk["closures"] and chk["closure_beats_plain"]
