@@ -104,6 +104,19 @@ __device__ __forceinline__ int face_neighbour(int e, int f, int nx, int ny, int 
   return ix + nx * (iy + ny * iz);
 }
 
+// Cyclic relabelling of the axes that takes direction l to x: axis k of the
+// rotated frame is axis (k + l) mod 3 of the mesh.  The face kernels
+// evaluate the Roe and viscous face fluxes of every face in the rotated
+// frame, with the x-direction form of the flux, and apply the relabelling
+// to the load and store addresses.  A warp's threads hold faces of
+// different directions; with one code path for all of them the warp does
+// not diverge (per-direction code paths ran one after the other).  The
+// fluxes are invariant under the rotation: only the order of the terms of a
+// few three-term sums (|v|^2, v.dm, tau_i v_i) changes.
+__device__ __forceinline__ int rot_axis(int k, int l) { return k + l >= 3 ? k + l - 3 : k + l; }
+// variable v of the rotated frame -> the same variable in the mesh frame
+__device__ __forceinline__ int rot_var(int v, int l) { return (v == 0 || v == 4) ? v : 1 + rot_axis(v - 1, l); }
+
 // Non-finite test on the exponent bits (integer pipe, not the FP64 pipe).
 __device__ __forceinline__ bool not_finite(double x) {
   return (__double_as_longlong(x) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;

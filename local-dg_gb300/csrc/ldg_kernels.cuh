@@ -225,6 +225,7 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
   // Roe flux on the three minus faces (numericalFluxC, solver.cpp:1194-1374):
   // each face is computed once, here, by the element on its plus side; the
   // element on the minus side uses its negation (the flux is antisymmetric).
+  // Every face in the frame where its normal is x (rot_var).
   for (int i = threadIdx.x; i < ne * 3 * nf; i += NT) {
     const int es2 = i / (3 * nf);
     const int r = i - es2 * 3 * nf;
@@ -232,14 +233,13 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
     T uK[kNS], uN[kNS], F[kNS];
 #pragma unroll
     for (int v = 0; v < kNS; ++v) {
-      uK[v] = sTo[((es2 * 3 + l) * kNS + v) * nf + t];
-      uN[v] = sTm[((es2 * 3 + l) * kNS + v) * nf + t];
+      const int vm = rot_var(v, l);
+      uK[v] = sTo[((es2 * 3 + l) * kNS + vm) * nf + t];
+      uN[v] = sTm[((es2 * 3 + l) * kNS + vm) * nf + t];
     }
-    if (l == 0) roe_flux<0>(uN, uK, false, o, F);
-    else if (l == 1) roe_flux<1>(uN, uK, false, o, F);
-    else roe_flux<2>(uN, uK, false, o, F);
+    roe_flux<0>(uN, uK, false, o, F);
 #pragma unroll
-    for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + v * nf + t, F[v]);
+    for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + rot_var(v, l) * nf + t, F[v]);
   }
   __syncthreads();  // the own -l traces are dead: Q takes their space
   const int es = threadIdx.x / n, q = threadIdx.x % n;
@@ -449,32 +449,41 @@ struct StageArgs {
 };
 
 // Numerical flux sum Fc* + Fv* at face point t of face f (direction L) of
-// element e, written to out[v*nf].
-template <int N, int L, class T>
+// element e, written to out[v*nf].  Evaluated in the frame where the face
+// normal is x (rot_var), so faces of all directions share one code path.
+template <int N, class T>
 __device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& ops, const OpsT<T>& o, long e,
                                           int f, int t, T* out) {
   constexpr int nf = N * N;
   using R = Real<T>;
   const bool plus = f & 1;
+  const int L = f >> 1;
   const long en = face_neighbour((int)e, f, ops.nx, ops.ny, ops.nz);
+  int vm[kNS];
+#pragma unroll
+  for (int v = 0; v < kNS; ++v) vm[v] = rot_var(v, L);
   T uK[kNS], Du[kNQ], Fc[kNS], Fv[kNS];
   const auto* tK = a.Tu + (e * 6 + f) * kNS * nf + t;
 #pragma unroll
-  for (int v = 0; v < kNS; ++v) uK[v] = R::ld(tK + v * nf);
+  for (int v = 0; v < kNS; ++v) uK[v] = R::ld(tK + vm[v] * nf);
   // Roe flux: own minus face, or the negated minus-face flux of the plus
   // neighbour
   const auto* fm = a.Fm + ((plus ? en : e) * 3 + L) * kNS * nf + t;
 #pragma unroll
-  for (int v = 0; v < kNS; ++v) Fc[v] = sgn(!plus, R::ld(fm + v * nf));
-  // q from the element on the plus side (numericalFluxV kWins switch)
+  for (int v = 0; v < kNS; ++v) Fc[v] = sgn(!plus, R::ld(fm + vm[v] * nf));
+  // q from the element on the plus side (numericalFluxV kWins switch);
+  // gradient direction j of the rotated frame is mesh direction
+  // rot_axis(j, L)
   const auto* tq = a.Tq + ((plus ? en : e) * 3 + L) * kNQ * nf + t;
 #pragma unroll
-  for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(tq + k * nf);
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int v = 0; v < kNS; ++v) Du[j * kNS + v] = R::ld(tq + (rot_axis(j, L) * kNS + vm[v]) * nf);
   ViscPre<T> P;
   visc_pre(uK, Du, P);
-  visc_column<L>(P, o, Fv);
+  visc_column<0>(P, o, Fv);
 #pragma unroll
-  for (int v = 0; v < kNS; ++v) out[v * nf] = Fc[v] - sgn(plus, Fv[v]);
+  for (int v = 0; v < kNS; ++v) out[vm[v] * nf] = Fc[v] - sgn(plus, Fv[v]);
 }
 
 template <int N, class T, int E = DefEPC<N>::value>
@@ -517,12 +526,7 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
     const int fes = j / (6 * nf);
     const int r = j - fes * 6 * nf;
     const int f = r / nf, t = r - f * nf;
-    T* out = sFs + (fes * 6 + f) * kNS * nf + t;
-    switch (f >> 1) {
-      case 0: face_flux<N, 0>(a, ops, o, e0 + fes, f, t, out); break;
-      case 1: face_flux<N, 1>(a, ops, o, e0 + fes, f, t, out); break;
-      default: face_flux<N, 2>(a, ops, o, e0 + fes, f, t, out); break;
-    }
+    face_flux<N>(a, ops, o, e0 + fes, f, t, sFs + (fes * 6 + f) * kNS * nf + t);
   };
   if constexpr (std::is_same<T, dd>::value) {
     // The FP32-pair path is latency-bound: one work list over both kinds
