@@ -230,11 +230,12 @@ int ldg_probe_fp64_peak(int device, double* tflops);
  * SM clock the probe ran at, in MHz (cycles over event time).  Either
  * pointer may be NULL.  (No reference counterpart.) */
 int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* sm_mhz);
-/* Applies the flux kernels' FP64 reciprocal and reciprocal square root
- * (an FP32 special-function seed and one third-order correction) to the n
- * host operands x, writing 1/x to r and 1/sqrt(x) to rs (host buffers).
- * For checking them against correctly rounded values.  (No reference
- * counterpart: the reference divides and calls sqrt, solver.cpp:1291-1372.) */
+/* Applies the flux kernels' FP64 reciprocal (an FP32 special-function seed
+ * and one third-order correction) and reciprocal square root (CUDA's
+ * rsqrt) to the n host operands x, writing 1/x to r and 1/sqrt(x) to rs
+ * (host buffers).  For checking them against correctly rounded values.
+ * (No reference counterpart: the reference divides and calls sqrt,
+ * solver.cpp:1291-1372.) */
 int ldg_probe_recip(int device, const double* x, double* r, double* rs, long n);
 /* Measures the gradient pass's volume contraction alone (the product the
  * reference evaluates as a dense DGEMM, solver.cpp:500, here the

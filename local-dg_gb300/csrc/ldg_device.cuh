@@ -122,23 +122,23 @@ __device__ __forceinline__ bool not_finite(double x) {
   return (__double_as_longlong(x) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
 }
 
-// FP64 reciprocal and reciprocal square root of the flux formulas, faithful
-// (within one ulp; ldg_probe_recip measures them against 1.0/x and rsqrt).
-// The flux kernels are FP64-pipe bound, so these spend as few FP64
-// instructions as they can:
+// FP64 reciprocal of the flux formulas, faithful (within one ulp;
+// ldg_probe_recip measures it against 1.0/x).  The flux kernels are FP64-pipe
+// bound, so it spends as few FP64 instructions as it can:
 //   * seed: the FP32 special-function approximation, applied to x truncated
 //     to 23 mantissa bits.  The operand goes into and the seed y0 comes out
 //     of FP32 by rebiasing the exponent field with integer instructions
 //     (an exact change of format, no FP64 or conversion instruction);
 //     relative error below 2^-21;
-//   * one third-order (Householder) correction with e the seed's residual:
-//       1/x:        e = 1 - x y0,    y = y0 (1 + e + e^2)           3 DFMA
-//       1/sqrt(x):  e = 1 - x y0^2,  y = y0 (1 + e/2 + 3e^2/8)      3 DFMA + 2 DMUL
-//     leaving e^3 (resp. 5e^3/16), below 2^-60, plus the last rounding.
-//     y0 has 24 significant bits, so y0^2 is exact in FP64.
+//   * one third-order (Householder) correction with e = 1 - x y0, the
+//     seed's residual: y = y0 (1 + e + e^2), three DFMA, leaving e^3
+//     (below 2^-60) plus the last rounding.
 // Outside [2^-125, 2^126) (zero, negative, non-finite, FP32-subnormal or
-// huge operands) CUDA's 1.0/x and rsqrt take over, so every special case
-// keeps IEEE behaviour.
+// huge operands) CUDA's 1.0/x takes over, so every special case keeps IEEE
+// behaviour.  Measured at 64^3 p=4: the RHS pass 20.30 -> 20.04 ms against
+// 1.0/x.  The same construction for 1/sqrt(x) (the series 1 + e/2 + 3e^2/8,
+// three DFMA and two DMUL) was 1.4 % slower in the gradient pass than
+// CUDA's rsqrt, which the flux code keeps.
 namespace recip_detail {
 constexpr unsigned kRebias = (1023u - 127u) << 20;  // exponent bias difference in the high word
 
@@ -159,12 +159,6 @@ __device__ __forceinline__ float rcp_approx(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
-
-__device__ __forceinline__ float rsqrt_approx(float x) {
-  float r;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
 }  // namespace recip_detail
 
 __device__ __forceinline__ double rcp(double x) {
@@ -175,18 +169,12 @@ __device__ __forceinline__ double rcp(double x) {
   return fma(y0, fma(e, e, e), y0);
 }
 
-__device__ __forceinline__ double rsqrt_(double x) {
-  const int hi = __double2hiint(x), lo = __double2loint(x);
-  if (__builtin_expect(!recip_detail::in_range(hi), 0)) return ::rsqrt(x);
-  const double y0 = recip_detail::to_f64(recip_detail::rsqrt_approx(recip_detail::to_f32(hi, lo)));
-  const double e = fma(-x, y0 * y0, 1.0);
-  return fma(y0, e * fma(e, 0.375, 0.5), y0);
-}
+// 1/sqrt(x): CUDA's double rsqrt; on the FP32-pair path the pair reciprocal
+// of the pair square root.
+__device__ __forceinline__ double rsqrt_(double x) { return ::rsqrt(x); }
 
 // helpers that are exact in both types
 __device__ __forceinline__ double half_(double x) { return 0.5 * x; }
-// 1/sqrt(x) on the FP32-pair path: the pair reciprocal of the pair square
-// root.
 __device__ __forceinline__ dd rsqrt_(dd x) { return rcp(sqrt(x)); }
 __device__ __forceinline__ dd half_(dd x) { return scale2(x, 0.5f); }
 template <class T>

@@ -1,8 +1,9 @@
-"""The flux kernels' FP64 reciprocal and reciprocal square root (an FP32
-special-function seed with one third-order correction, ldg_device.cuh)
-against correctly rounded values: faithful (below one ulp) wherever the
-seeded form runs, and IEEE behaviour (CUDA's own 1.0/x and rsqrt) on zero,
-negative, non-finite, subnormal and out-of-range operands."""
+"""The flux kernels' FP64 reciprocal (an FP32 special-function seed with one
+third-order correction, ldg_device.cuh) against correctly rounded values:
+faithful (below one ulp) wherever the seeded form runs, and IEEE behaviour
+(CUDA's own 1.0/x) on zero, negative, non-finite, subnormal and
+out-of-range operands.  The reciprocal square root the fluxes use is CUDA's
+rsqrt, checked against its documented bound (one ulp)."""
 import numpy as np
 import pytest
 
@@ -42,9 +43,9 @@ def test_faithful_in_the_seeded_range(operands):
     r, rs = ldg.probe_recip(x)
     er, ers = ulp_error(r, x, recip), ulp_error(rs, x, rsqrt)
     assert er.max() < 1.0, (er.max(), x[er.argmax()])
-    assert ers.max() < 1.0, (ers.max(), x[ers.argmax()])
     # almost always the correctly rounded value
-    assert np.mean(er <= 0.5) > 0.99 and np.mean(ers <= 0.5) > 0.99
+    assert np.mean(er <= 0.5) > 0.99
+    assert ers.max() <= 1.0, (ers.max(), x[ers.argmax()])
 
 
 def test_special_and_out_of_range_operands():
