@@ -50,11 +50,11 @@ BYTES_RHS = 8 * (5 + 15 + 5)     # read U, read q, write k / next stage
 # kernels at 24^3 p=4 (13,824 elements; DRAM traffic and instruction counts
 # grow in proportion to the element count): DRAM bytes read + written, and
 # FP64 floating-point operations executed (2 per DFMA, 1 per DMUL or DADD;
-# k_grad: 20,550 DFMA + 5,550 DMUL + 2,925 DADD; k_rhs: 28,800 + 6,000 +
-# 3,300).
+# k_grad: 20,400 DFMA + 5,550 DMUL + 2,925 DADD; k_rhs: 28,300 + 5,950 +
+# 3,250).
 NCU_PER_ELEMENT = {
-    ("grad", 5, "fp64"): {"dram_bytes": (152.824320e6 + 313.398784e6) / 13824, "fp64_flops": 49575.0},
-    ("rhs", 5, "fp64"): {"dram_bytes": (649.381632e6 + 189.743360e6) / 13824, "fp64_flops": 66900.0},
+    ("grad", 5, "fp64"): {"dram_bytes": (153.257216e6 + 316.232192e6) / 13824, "fp64_flops": 49275.0},
+    ("rhs", 5, "fp64"): {"dram_bytes": (649.352960e6 + 189.280256e6) / 13824, "fp64_flops": 65800.0},
     ("grad", 5, "mixed"): {"dram_bytes": (152.870400e6 + 312.989952e6) / 13824},
     ("rhs", 5, "mixed"): {"dram_bytes": (649.710080e6 + 189.202176e6) / 13824},
 }
