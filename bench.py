@@ -53,8 +53,10 @@ BYTES_RHS = 8 * (5 + 15 + 5)     # read U, read q, write k / next stage
 # k_grad: 20,400 DFMA + 5,550 DMUL + 2,925 DADD; k_rhs: 28,300 + 5,950 +
 # 3,250).
 NCU_PER_ELEMENT = {
-    ("grad", 5, "fp64"): {"dram_bytes": (153.257216e6 + 316.232192e6) / 13824, "fp64_flops": 49275.0},
-    ("rhs", 5, "fp64"): {"dram_bytes": (649.352960e6 + 189.280256e6) / 13824, "fp64_flops": 65800.0},
+    ("grad", 5, "fp64"): {"dram_bytes": (153.257216e6 + 316.232192e6) / 13824, "fp64_flops": 49275.0,
+                          "fp64_pipe_ops": 20400.0 + 5550.0 + 2925.0},
+    ("rhs", 5, "fp64"): {"dram_bytes": (649.352960e6 + 189.280256e6) / 13824, "fp64_flops": 65800.0,
+                         "fp64_pipe_ops": 28300.0 + 5950.0 + 3250.0},
     ("grad", 5, "mixed"): {"dram_bytes": (152.870400e6 + 312.989952e6) / 13824},
     ("rhs", 5, "mixed"): {"dram_bytes": (649.710080e6 + 189.202176e6) / 13824},
 }
@@ -562,6 +564,17 @@ def run_ours(args):
                                     "probe": pr, "derived_peak_tflops": derived,
                                     "flops_per_dof": ncu["fp64_flops"] / N ** 3,
                                     "flops_source": "ncu instruction counts, 24^3 p=4 capture"}
+        # The same in FP64 pipe instructions: a DMUL or DADD takes a pipe slot
+        # as a DFMA does but counts one flop, so flops understate how busy
+        # the pipe is.  Instructions per SM per clock (at the sampled SM
+        # clock) against the probe's FMAs per SM per clock.
+        clk = (clocks or {}).get("sm_mhz") or max_mhz
+        per_clk = ncu["fp64_pipe_ops"] * s.nE / avg_s / (props.multi_processor_count * clk * 1e6)
+        roofline["binding_roof"]["pipe_issue"] = {
+            "fp64_instructions_per_sm_clk": per_clk, "probe_fma_per_sm_clk": pr["fma_per_sm_clk"],
+            "frac_of_probe": per_clk / pr["fma_per_sm_clk"], "sm_mhz": clk,
+            "instructions_per_element": ncu["fp64_pipe_ops"],
+            "source": "DFMA + DMUL + DADD per element from the same ncu capture"}
     kernel_ms = {k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1)} for k, v in kt.items()}
     contraction = None
     if args.precision == "fp64" and not args.no_variants and args.p == 4:
