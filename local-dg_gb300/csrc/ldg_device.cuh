@@ -274,12 +274,16 @@ __device__ __forceinline__ void sub_visc_column(const ViscPre<T>& P, const OpsT<
   F[4] = fma(tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + o.kappa * P.de[j], mre, F[4]);
 }
 
-// Roe flux F*(uN, uK, n) seen from element K with n = s e_l
+// Roe flux F*(uN, uK, n) seen from element K with n = s e_x
 // (numericalFluxC, solver.cpp:1291-1372): central flux minus Roe-averaged
-// upwind dissipation; the reference's hard-coded 0.4 is g1.
-template <int l, class T>
-__device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool s, const OpsT<T>& o,
-                                         T F[kNS]) {
+// upwind dissipation; the reference's hard-coded 0.4 is g1.  Faces of the
+// other directions are evaluated in the frame where their normal is x
+// (rot_var).  The algebra is arranged for few operations: p from m.v, the
+// wave-strength combinations t179 = a1 dp/c^2 + a2 dq/c and t186 = a2 dp/c
+// + a1 dq with one 1/c, and the pressure term inside F[1]'s halving (a
+// scaling by 1/2 is exact, so half(a) + half(b) = half(a + b)).
+template <class T>
+__device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool s, const OpsT<T>& o, T F[kNS]) {
   T rN = uN[0], rK = uK[0];
   // One reciprocal square root s2 = 1/sqrt(rho_N rho_K) gives both inverse
   // densities (rho_K s2^2, rho_N s2^2) and the Roe weight sqrt(rho_N/rho_K)
@@ -289,36 +293,39 @@ __device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool 
   T irN = rK * ip, irK = rN * ip;
   T vN[3] = {uN[1] * irN, uN[2] * irN, uN[3] * irN};
   T vK[3] = {uK[1] * irK, uK[2] * irK, uK[3] * irK};
-  T qN = sgn(s, vN[l]), qK = sgn(s, vK[l]);
-  T pN = o.g1 * uN[4] - o.hg1 * rN * (vN[0] * vN[0] + vN[1] * vN[1] + vN[2] * vN[2]);
-  T pK = o.g1 * uK[4] - o.hg1 * rK * (vK[0] * vK[0] + vK[1] * vK[1] + vK[2] * vK[2]);
+  T qN = sgn(s, vN[0]), qK = sgn(s, vK[0]);
+  // p = g1 E - (g1/2) |m|^2 / rho, with |m|^2 / rho = m.v
+  T pN = o.g1 * uN[4] - o.hg1 * (uN[1] * vN[0] + uN[2] * vN[1] + uN[3] * vN[2]);
+  T pK = o.g1 * uK[4] - o.hg1 * (uK[1] * vK[0] + uK[2] * vK[1] + uK[3] * vK[2]);
+  T EpN = uN[4] + pN, EpK = uK[4] + pK;
   T sq = rN * s2;
   T is1 = rcp(sq + o.one);
   T vt[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) vt[i] = (sq * vN[i] + vK[i]) * is1;
-  T Ht = (sq * (uN[4] + pN) * irN + (uK[4] + pK) * irK) * is1;
-  T vt2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
-  T qt = sgn(s, vt[l]);
-  T c2 = o.g1 * (Ht - half_(vt2));
+  T Ht = (sq * (EpN * irN) + EpK * irK) * is1;
+  T hv2 = half_(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+  T qt = sgn(s, vt[0]);
+  T c2 = o.g1 * (Ht - hv2);
   T ic = rsqrt_(c2);  // 1/c
   T c = c2 * ic;
-  T ic2 = ic * ic;
   T l0 = fabs(qt);
-  T lp = half_(fabs(qt + c)), lm = half_(fabs(c - qt));
+  // eigenvalue combinations a1 = (|qt+c| + |c-qt|)/2 - |qt|, a2 = (|qt+c| - |c-qt|)/2
+  T A = fabs(qt + c), B = fabs(c - qt);
+  T a1 = half_(A + B) - l0, a2 = half_(A - B);
   T dr = rN - rK;
   T dm[3] = {uN[1] - uK[1], uN[2] - uK[2], uN[3] - uK[3]};
   T dE = uN[4] - uK[4];
-  T a1 = lp + lm - l0, a2 = lp - lm;
-  T dp = o.g1 * (half_(vt2) * dr - (vt[0] * dm[0] + vt[1] * dm[1] + vt[2] * dm[2]) + dE);
-  T dq = sgn(s, dm[l]) - qt * dr;
-  T t179 = a1 * dp * ic2 + a2 * dq * ic;
-  T t186 = a2 * dp * ic + a1 * dq;
+  T dp = o.g1 * (hv2 * dr - (vt[0] * dm[0] + vt[1] * dm[1] + vt[2] * dm[2]) + dE);
+  T dq = sgn(s, dm[0]) - qt * dr;
+  T dpi = dp * ic;
+  T t179 = (a1 * dpi + a2 * dq) * ic;
+  T t186 = a2 * dpi + a1 * dq;
   F[0] = half_(rN * qN + rK * qK - l0 * dr - t179);
+  F[1] = half_(uN[1] * qN + uK[1] * qK - l0 * dm[0] - t179 * vt[0] + sgn(s, pN + pK - t186));
 #pragma unroll
-  for (int i = 0; i < 3; ++i) F[1 + i] = half_(uN[1 + i] * qN + uK[1 + i] * qK - l0 * dm[i] - t179 * vt[i]);
-  F[1 + l] += half_(sgn(s, pN + pK - t186));
-  F[4] = half_((uN[4] + pN) * qN + (uK[4] + pK) * qK - l0 * dE - t179 * Ht - t186 * qt);
+  for (int i = 1; i < 3; ++i) F[1 + i] = half_(uN[1 + i] * qN + uK[1 + i] * qK - l0 * dm[i] - t179 * vt[i]);
+  F[4] = half_(EpN * qN + EpK * qK - l0 * dE - t179 * Ht - t186 * qt);
 }
 
 }  // namespace ldg

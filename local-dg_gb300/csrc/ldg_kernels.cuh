@@ -237,7 +237,7 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
       uK[v] = sTo[((es2 * 3 + l) * kNS + vm) * nf + t];
       uN[v] = sTm[((es2 * 3 + l) * kNS + vm) * nf + t];
     }
-    roe_flux<0>(uN, uK, false, o, F);
+    roe_flux(uN, uK, false, o, F);
 #pragma unroll
     for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + rot_var(v, l) * nf + t, F[v]);
   }
@@ -263,10 +263,11 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
         const T tm = sTm[((es * 3 + l) * kNS + v) * nf + t];
         T g;
         if constexpr (std::is_same<T, double>::value) {
-          T acc{};
+          // the lifts first, then the volume terms: seven FP64 operations
+          T acc = fma(-lm, tm, lp * tp);
 #pragma unroll
-          for (int r = 0; r < N; ++r) acc = fma(row[r], line[r * st], acc);
-          g = lp * tp - lm * tm - acc;
+          for (int r = 0; r < N; ++r) acc = fma(-row[r], line[r * st], acc);
+          g = acc;
         } else {  // one compensated 7-term dot product
           Acc<T> acc;
 #pragma unroll
