@@ -182,33 +182,40 @@ __device__ __forceinline__ T sgn(bool plus, T x) { return plus ? x : -x; }
 
 // Euler flux, column l of F(u): components (rho, m_x, m_y, m_z, E) of the
 // flux in direction l (solver.cpp:1060-1084 with fluxes[iS + 5 l]).
-// ir = 1/rho; p = g1 (E - |m|^2/(2 rho)); energy flux m_l (E + p)/rho, with
-// E + p written gamma E - g1|m|^2/(2rho) as the reference does.
+// p = g1 (E - |m|^2/(2 rho)); energy flux m_l (E + p)/rho, with E + p
+// written gamma E - g1|m|^2/(2rho) as the reference does.  With v = m/rho
+// given: the momentum flux m_i v_l is symmetric in (i, l) (both equal
+// rho v_i v_l), so six products give its nine entries, and its diagonal
+// gives |m|^2/rho.
 template <class T>
 struct Euler {
-  T ir, p, h;  // 1/rho, pressure, (E+p)/rho
+  T p, h;  // pressure, (E+p)/rho
+  T M[6];  // m_i v_l: xx, yx, zx, yy, zy, zz
 };
 
 template <class T>
-__device__ __forceinline__ Euler<T> euler_state(const T u[kNS], const OpsT<T>& o) {
+__device__ __forceinline__ Euler<T> euler_state(const T u[kNS], T ir, const T v[3], const OpsT<T>& o) {
   Euler<T> s;
-  s.ir = rcp(u[0]);
-  T k = (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) * s.ir * o.hg1;
+  s.M[0] = u[1] * v[0];
+  s.M[1] = u[2] * v[0];
+  s.M[2] = u[3] * v[0];
+  s.M[3] = u[2] * v[1];
+  s.M[4] = u[3] * v[1];
+  s.M[5] = u[3] * v[2];
+  T k = o.hg1 * (s.M[0] + s.M[3] + s.M[5]);
   s.p = o.g1 * u[4] - k;
-  s.h = (o.gamma * u[4] - k) * s.ir;
+  s.h = (o.gamma * u[4] - k) * ir;
   return s;
 }
 
-template <class T>
-__device__ __forceinline__ void euler_column(const T u[kNS], const Euler<T>& s, int l, T F[kNS]) {
-  T ml = u[1 + l];
-  T vl = ml * s.ir;
-  F[0] = ml;
-  F[1] = u[1] * vl;
-  F[2] = u[2] * vl;
-  F[3] = u[3] * vl;
+template <int l, class T>
+__device__ __forceinline__ void euler_column(const T u[kNS], const Euler<T>& s, T F[kNS]) {
+  F[0] = u[1 + l];
+  F[1] = s.M[l == 0 ? 0 : l == 1 ? 1 : 2];
+  F[2] = s.M[l == 0 ? 1 : l == 1 ? 3 : 4];
+  F[3] = s.M[l == 0 ? 2 : l == 1 ? 4 : 5];
   F[1 + l] += s.p;
-  F[4] = ml * s.h;
+  F[4] = u[1 + l] * s.h;
 }
 
 // Velocity gradient G[i][j] = d_j v_i from u and Du[c], c = j*5 + var
@@ -245,33 +252,21 @@ __device__ __forceinline__ void visc_pre(const T u[kNS], const T* Du, ViscPre<T>
   visc_pre(u, rcp(u[0]), Du, P);
 }
 
-// Column j of the viscous flux (solver.cpp:1136-1187): Newtonian stress with
-// Stokes' hypothesis over Re, heat flux (gamma/Pr) grad e / Re.
+// F += c Re * (column j of the viscous flux) (solver.cpp:1136-1187):
+// Newtonian stress with Stokes' hypothesis over Re, heat flux (gamma/Pr)
+// grad e / Re; c = -1/Re subtracts it from the Euler column (volume), c =
+// +-1/Re adds the signed face flux to the Roe flux (faces).  Fused into
+// FMAs; F[0] gets no viscous part.
 template <int j, class T>
-__device__ __forceinline__ void visc_column(const ViscPre<T>& P, const OpsT<T>& o, T F[kNS]) {
+__device__ __forceinline__ void add_visc_column(const ViscPre<T>& P, const T c, const OpsT<T>& o, T F[kNS]) {
   T tau[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) tau[i] = P.G[i][j] + P.G[j][i];
   tau[j] -= o.two3 * P.div;
-  F[0] = T{};
-  F[1] = tau[0] * o.inv_re;
-  F[2] = tau[1] * o.inv_re;
-  F[3] = tau[2] * o.inv_re;
-  F[4] = (tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + o.kappa * P.de[j]) * o.inv_re;
-}
-
-// F -= column j of the viscous flux, fused (FMA) into the Euler column.
-template <int j, class T>
-__device__ __forceinline__ void sub_visc_column(const ViscPre<T>& P, const OpsT<T>& o, T F[kNS]) {
-  T tau[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) tau[i] = P.G[i][j] + P.G[j][i];
-  tau[j] -= o.two3 * P.div;
-  const T mre = -o.inv_re;
-  F[1] = fma(tau[0], mre, F[1]);
-  F[2] = fma(tau[1], mre, F[2]);
-  F[3] = fma(tau[2], mre, F[3]);
-  F[4] = fma(tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + o.kappa * P.de[j], mre, F[4]);
+  F[1] = fma(tau[0], c, F[1]);
+  F[2] = fma(tau[1], c, F[2]);
+  F[3] = fma(tau[2], c, F[3]);
+  F[4] = fma(tau[0] * P.v[0] + tau[1] * P.v[1] + tau[2] * P.v[2] + o.kappa * P.de[j], c, F[4]);
 }
 
 // Roe flux F*(uN, uK, n) seen from element K with n = s e_x

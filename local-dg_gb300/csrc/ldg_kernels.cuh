@@ -463,7 +463,7 @@ __device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& o
   int vm[kNS];
 #pragma unroll
   for (int v = 0; v < kNS; ++v) vm[v] = rot_var(v, L);
-  T uK[kNS], Du[kNQ], Fc[kNS], Fv[kNS];
+  T uK[kNS], Du[kNQ], F[kNS];
   const auto* tK = a.Tu + (e * 6 + f) * kNS * nf + t;
 #pragma unroll
   for (int v = 0; v < kNS; ++v) uK[v] = R::ld(tK + vm[v] * nf);
@@ -471,7 +471,7 @@ __device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& o
   // neighbour
   const auto* fm = a.Fm + ((plus ? en : e) * 3 + L) * kNS * nf + t;
 #pragma unroll
-  for (int v = 0; v < kNS; ++v) Fc[v] = sgn(!plus, R::ld(fm + vm[v] * nf));
+  for (int v = 0; v < kNS; ++v) F[v] = sgn(!plus, R::ld(fm + vm[v] * nf));
   // q from the element on the plus side (numericalFluxV kWins switch);
   // gradient direction j of the rotated frame is mesh direction
   // rot_axis(j, L)
@@ -482,9 +482,10 @@ __device__ __forceinline__ void face_flux(const StageArgs<T>& a, const DevOps& o
     for (int v = 0; v < kNS; ++v) Du[j * kNS + v] = R::ld(tq + (rot_axis(j, L) * kNS + vm[v]) * nf);
   ViscPre<T> P;
   visc_pre(uK, Du, P);
-  visc_column<0>(P, o, Fv);
+  // Fc* + Fv*, Fv* = -s Fv_x: the viscous column enters with -s/Re
+  add_visc_column<0>(P, plus ? -o.inv_re : o.inv_re, o, F);
 #pragma unroll
-  for (int v = 0; v < kNS; ++v) out[vm[v] * nf] = Fc[v] - sgn(plus, Fv[v]);
+  for (int v = 0; v < kNS; ++v) out[vm[v] * nf] = F[v];
 }
 
 template <int N, class T, int E = DefEPC<N>::value>
@@ -509,19 +510,24 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
     for (int v = 0; v < kNS; ++v) u[v] = R::ld(a.Us + (e * kNS + v) * n + q2);
 #pragma unroll
     for (int k = 0; k < kNQ; ++k) Du[k] = R::ld(a.Q + (e * kNQ + k) * n + q2);
-    Euler<T> es_ = euler_state(u, o);
+    const T ir = rcp(u[0]);
     ViscPre<T> P;
-    visc_pre(u, es_.ir, Du, P);
+    visc_pre(u, ir, Du, P);
+    const Euler<T> es_ = euler_state(u, ir, P.v, o);
+    const T mre = -o.inv_re;
+    T F[kNS];
+    euler_column<0>(u, es_, F);
+    add_visc_column<0>(P, mre, o, F);
 #pragma unroll
-    for (int l = 0; l < 3; ++l) {
-      T F[kNS];
-      euler_column(u, es_, l, F);
-      if (l == 0) sub_visc_column<0>(P, o, F);
-      else if (l == 1) sub_visc_column<1>(P, o, F);
-      else sub_visc_column<2>(P, o, F);
+    for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + 0 * kNS + v) * n + q2] = F[v];
+    euler_column<1>(u, es_, F);
+    add_visc_column<1>(P, mre, o, F);
 #pragma unroll
-      for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + l * kNS + v) * n + q2] = F[v];
-    }
+    for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + 1 * kNS + v) * n + q2] = F[v];
+    euler_column<2>(u, es_, F);
+    add_visc_column<2>(P, mre, o, F);
+#pragma unroll
+    for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + 2 * kNS + v) * n + q2] = F[v];
   };
   auto face_item = [&](int j) {
     const int fes = j / (6 * nf);
