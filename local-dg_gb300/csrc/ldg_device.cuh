@@ -180,41 +180,59 @@ __device__ __forceinline__ dd half_(dd x) { return scale2(x, 0.5f); }
 template <class T>
 __device__ __forceinline__ T sgn(bool plus, T x) { return plus ? x : -x; }
 
+// a*b rounded on its own, never fused into a neighbouring sum.  A product
+// that several sums use must round the same way in every kernel that
+// inlines this code (the solo kernels and the ensemble's tiles are
+// separate instantiations, and results must agree bit for bit); whether
+// the compiler fuses such a product into one of its sums is its own choice
+// per instantiation, so those products are pinned.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ dd mul_rn(dd a, dd b) { return a * b; }
+__device__ __forceinline__ double half_rn(double x) { return __dmul_rn(0.5, x); }
+__device__ __forceinline__ dd half_rn(dd x) { return half_(x); }
+
 // Euler flux, column l of F(u): components (rho, m_x, m_y, m_z, E) of the
 // flux in direction l (solver.cpp:1060-1084 with fluxes[iS + 5 l]).
 // p = g1 (E - |m|^2/(2 rho)); energy flux m_l (E + p)/rho, with E + p
 // written gamma E - g1|m|^2/(2rho) as the reference does.  With v = m/rho
-// given: the momentum flux m_i v_l is symmetric in (i, l) (both equal
-// rho v_i v_l), so six products give its nine entries, and its diagonal
-// gives |m|^2/rho.
+// given: |m|^2/rho = m.v, the diagonal momentum flux plus pressure is one
+// FMA m_l v_l + p, and the momentum flux m_i v_l is symmetric in (i, l)
+// (both equal rho v_i v_l), so three products give its six off-diagonal
+// entries.  Every sum is an explicit FMA or takes unfused operands.
 template <class T>
 struct Euler {
   T p, h;  // pressure, (E+p)/rho
-  T M[6];  // m_i v_l: xx, yx, zx, yy, zy, zz
+  T M[3];  // off-diagonal m_i v_l: xy, xz, yz
 };
 
 template <class T>
 __device__ __forceinline__ Euler<T> euler_state(const T u[kNS], T ir, const T v[3], const OpsT<T>& o) {
   Euler<T> s;
-  s.M[0] = u[1] * v[0];
-  s.M[1] = u[2] * v[0];
-  s.M[2] = u[3] * v[0];
-  s.M[3] = u[2] * v[1];
-  s.M[4] = u[3] * v[1];
-  s.M[5] = u[3] * v[2];
-  T k = o.hg1 * (s.M[0] + s.M[3] + s.M[5]);
-  s.p = o.g1 * u[4] - k;
-  s.h = (o.gamma * u[4] - k) * ir;
+  s.M[0] = u[2] * v[0];
+  s.M[1] = u[3] * v[0];
+  s.M[2] = u[3] * v[1];
+  const T k = o.hg1 * fma(u[3], v[2], fma(u[2], v[1], u[1] * v[0]));
+  s.p = fma(o.g1, u[4], -k);
+  s.h = fma(o.gamma, u[4], -k) * ir;
   return s;
 }
 
 template <int l, class T>
-__device__ __forceinline__ void euler_column(const T u[kNS], const Euler<T>& s, T F[kNS]) {
+__device__ __forceinline__ void euler_column(const T u[kNS], const T v[3], const Euler<T>& s, T F[kNS]) {
   F[0] = u[1 + l];
-  F[1] = s.M[l == 0 ? 0 : l == 1 ? 1 : 2];
-  F[2] = s.M[l == 0 ? 1 : l == 1 ? 3 : 4];
-  F[3] = s.M[l == 0 ? 2 : l == 1 ? 4 : 5];
-  F[1 + l] += s.p;
+  if constexpr (l == 0) {
+    F[1] = fma(u[1], v[0], s.p);
+    F[2] = s.M[0];
+    F[3] = s.M[1];
+  } else if constexpr (l == 1) {
+    F[1] = s.M[0];
+    F[2] = fma(u[2], v[1], s.p);
+    F[3] = s.M[2];
+  } else {
+    F[1] = s.M[1];
+    F[2] = s.M[2];
+    F[3] = fma(u[3], v[2], s.p);
+  }
   F[4] = u[1 + l] * s.h;
 }
 
@@ -240,7 +258,7 @@ __device__ __forceinline__ void visc_pre(const T u[kNS], const T ir, const T* Du
   for (int j = 0; j < 3; ++j) {
     T dr = Du[j * kNS + 0];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) P.G[i][j] = (Du[j * kNS + 1 + i] - dr * P.v[i]) * ir;
+    for (int i = 0; i < 3; ++i) P.G[i][j] = mul_rn(Du[j * kNS + 1 + i] - dr * P.v[i], ir);
     P.de[j] = (Du[j * kNS + 4] - dr * eo) * ir -
               (P.v[0] * P.G[0][j] + P.v[1] * P.G[1][j] + P.v[2] * P.G[2][j]);
   }
@@ -293,17 +311,18 @@ __device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool 
   T pN = o.g1 * uN[4] - o.hg1 * (uN[1] * vN[0] + uN[2] * vN[1] + uN[3] * vN[2]);
   T pK = o.g1 * uK[4] - o.hg1 * (uK[1] * vK[0] + uK[2] * vK[1] + uK[3] * vK[2]);
   T EpN = uN[4] + pN, EpK = uK[4] + pK;
-  T sq = rN * s2;
+  // Products that several sums use are pinned (mul_rn): see mul_rn.
+  T sq = mul_rn(rN, s2);
   T is1 = rcp(sq + o.one);
   T vt[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) vt[i] = (sq * vN[i] + vK[i]) * is1;
-  T Ht = (sq * (EpN * irN) + EpK * irK) * is1;
-  T hv2 = half_(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+  for (int i = 0; i < 3; ++i) vt[i] = mul_rn(fma(sq, vN[i], vK[i]), is1);
+  T Ht = mul_rn(fma(sq, EpN * irN, EpK * irK), is1);
+  T hv2 = half_rn(fma(vt[2], vt[2], fma(vt[1], vt[1], vt[0] * vt[0])));
   T qt = sgn(s, vt[0]);
   T c2 = o.g1 * (Ht - hv2);
   T ic = rsqrt_(c2);  // 1/c
-  T c = c2 * ic;
+  T c = mul_rn(c2, ic);
   T l0 = fabs(qt);
   // eigenvalue combinations a1 = (|qt+c| + |c-qt|)/2 - |qt|, a2 = (|qt+c| - |c-qt|)/2
   T A = fabs(qt + c), B = fabs(c - qt);
@@ -314,7 +333,7 @@ __device__ __forceinline__ void roe_flux(const T uN[kNS], const T uK[kNS], bool 
   T dp = o.g1 * (hv2 * dr - (vt[0] * dm[0] + vt[1] * dm[1] + vt[2] * dm[2]) + dE);
   T dq = sgn(s, dm[0]) - qt * dr;
   T dpi = dp * ic;
-  T t179 = (a1 * dpi + a2 * dq) * ic;
+  T t179 = mul_rn(fma(a1, dpi, a2 * dq), ic);
   T t186 = a2 * dpi + a1 * dq;
   F[0] = half_(rN * qN + rK * qK - l0 * dr - t179);
   F[1] = half_(uN[1] * qN + uK[1] * qK - l0 * dm[0] - t179 * vt[0] + sgn(s, pN + pK - t186));

@@ -516,15 +516,15 @@ __device__ __forceinline__ void rhs_body(const StageArgs<T>& a, const DevOps& op
     const Euler<T> es_ = euler_state(u, ir, P.v, o);
     const T mre = -o.inv_re;
     T F[kNS];
-    euler_column<0>(u, es_, F);
+    euler_column<0>(u, P.v, es_, F);
     add_visc_column<0>(P, mre, o, F);
 #pragma unroll
     for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + 0 * kNS + v) * n + q2] = F[v];
-    euler_column<1>(u, es_, F);
+    euler_column<1>(u, P.v, es_, F);
     add_visc_column<1>(P, mre, o, F);
 #pragma unroll
     for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + 1 * kNS + v) * n + q2] = F[v];
-    euler_column<2>(u, es_, F);
+    euler_column<2>(u, P.v, es_, F);
     add_visc_column<2>(P, mre, o, F);
 #pragma unroll
     for (int v = 0; v < kNS; ++v) sF[(es2 * kNQ + 2 * kNS + v) * n + q2] = F[v];
