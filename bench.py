@@ -50,13 +50,13 @@ BYTES_RHS = 8 * (5 + 15 + 5)     # read U, read q, write k / next stage
 # kernels at 24^3 p=4 (13,824 elements; DRAM traffic and instruction counts
 # grow in proportion to the element count): DRAM bytes read + written, and
 # FP64 floating-point operations executed (2 per DFMA, 1 per DMUL or DADD;
-# k_grad: 20,250 DFMA + 5,175 DMUL + 1,200 DADD; k_rhs: 28,300 + 5,950 +
-# 3,250).
+# k_grad: 20,100 DFMA + 5,250 DMUL + 1,350 DADD; k_rhs: 27,925 + 5,450 +
+# 2,650).
 NCU_PER_ELEMENT = {
-    ("grad", 5, "fp64"): {"dram_bytes": (153.829632e6 + 320.442368e6) / 13824, "fp64_flops": 46875.0,
-                          "fp64_pipe_ops": 20250.0 + 5175.0 + 1200.0},
-    ("rhs", 5, "fp64"): {"dram_bytes": (649.352960e6 + 189.280256e6) / 13824, "fp64_flops": 65800.0,
-                         "fp64_pipe_ops": 28300.0 + 5950.0 + 3250.0},
+    ("grad", 5, "fp64"): {"dram_bytes": (154.009344e6 + 320.630272e6) / 13824, "fp64_flops": 46800.0,
+                          "fp64_pipe_ops": 20100.0 + 5250.0 + 1350.0},
+    ("rhs", 5, "fp64"): {"dram_bytes": (649.355776e6 + 189.405952e6) / 13824, "fp64_flops": 63950.0,
+                         "fp64_pipe_ops": 27925.0 + 5450.0 + 2650.0},
     ("grad", 5, "mixed"): {"dram_bytes": (152.870400e6 + 312.989952e6) / 13824},
     ("rhs", 5, "mixed"): {"dram_bytes": (649.710080e6 + 189.202176e6) / 13824},
 }
