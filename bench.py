@@ -340,7 +340,7 @@ def ensemble_variant(count, K, W, dev):
 
 CLOSURE_RECORDS = [os.path.join(ROOT, "local-dg_gb300", "examples", f)
                    for f in ("closure_c5_result.json", "closure_c5_loop_result.json", "closure_c5_loop2_result.json")]
-# The best variants re-judged against a fine run from an evaluation seed
+# The best variants evaluated again against a fine run from an evaluation seed
 # that neither training nor the choice of variant saw.
 CLOSURE_SEED_CHECK = os.path.join(ROOT, "local-dg_gb300", "examples", "closure_c5_seed3003_result.json")
 
@@ -388,7 +388,7 @@ def recorded_closure():
     """The a-posteriori accuracy of the fully trained closure from the
     committed records of the closure study: the best variant over the
     records on the main evaluation seed, against plain LDG on that seed, and
-    the best variants re-judged on a second evaluation seed.  None if a
+    the best variants evaluated again on a second evaluation seed.  None if a
     record is missing."""
     rec_out = None
     try:
