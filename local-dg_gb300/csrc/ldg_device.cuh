@@ -52,6 +52,21 @@ struct OpsT {
   T Lps[3][kDevMaxN], Lms[3][kDevMaxN];
   T Bi[kDevMaxN * kDevMaxN];  // Gauss -> CGL nodal (the KE quirk), Bi[i*N + q]
   T g1, hg1, gamma, inv_re, kappa, two3, one;
+  // The gradient along one line in pairwise form (FP64 gradient pass).  The
+  // Gauss points are symmetric, so As is skew-centrosymmetric
+  // (As[N-1-q][N-1-r] = -As[q][r]) and the lifts mirror (Lp[N-1-q] =
+  // Lm[q]).  With H = N/2, m = H (the middle point of odd N), and along the
+  // line e_r = x_r + x_{N-1-r}, o_r = x_r - x_{N-1-r} (r < H), tdif = tp - tm,
+  // tsum = tp + tm, the outputs q and N-1-q (q < H) are U + V and U - V:
+  //   U = gs[q] tdif - sum_r gp[q][r] o_r,
+  //   V = gd[q] tsum - sum_r gm[q][r] e_r - gm[q][H] x_m   (odd N),
+  // and the middle output is gc[H] tdif - sum_r gc[r] o_r (odd N), with
+  //   gs = (Lps + Lms)[q]/2, gd = (Lps - Lms)[q]/2,
+  //   gp[q][r] = (As[q][r] - As[q][N-1-r])/2, gm[q][r] = (As[q][r] + As[q][N-1-r])/2,
+  //   gm[q][H] = As[q][m], gc[r] = As[m][r], gc[H] = Lps[m].
+  T gs[3][kDevMaxN / 2], gd[3][kDevMaxN / 2];
+  T gp[3][kDevMaxN / 2][kDevMaxN / 2], gm[3][kDevMaxN / 2][kDevMaxN / 2 + 1];
+  T gc[3][kDevMaxN / 2 + 1];
 };
 
 // Host-side conversion of the double block into the arithmetic type T.
@@ -74,6 +89,32 @@ inline OpsT<T> make_opst(const DevOps& d, int N) {
     }
   }
   for (int i = 0; i < kDevMaxN * kDevMaxN; ++i) o.Bi[i] = host_cast(i < N * N ? d.Bi[i] : 0.0, tag);
+  const int H = N / 2;
+  for (int l = 0; l < 3; ++l) {
+    const long double ia = d.ia[l];
+    for (int q = 0; q < kDevMaxN / 2; ++q) {
+      const bool in = q < H;
+      o.gs[l][q] = host_cast(in ? (double)(((long double)d.Lp[q] + d.Lm[q]) * ia / 2) : 0.0, tag);
+      o.gd[l][q] = host_cast(in ? (double)(((long double)d.Lp[q] - d.Lm[q]) * ia / 2) : 0.0, tag);
+      for (int r = 0; r <= kDevMaxN / 2; ++r) {
+        double gp = 0.0, gm = 0.0;
+        if (in && r < H) {
+          gp = (double)(((long double)d.A[q * N + r] - d.A[q * N + N - 1 - r]) * ia / 2);
+          gm = (double)(((long double)d.A[q * N + r] + d.A[q * N + N - 1 - r]) * ia / 2);
+        } else if (in && r == H && (N & 1)) {
+          gm = (double)((long double)d.A[q * N + H] * ia);
+        }
+        if (r < kDevMaxN / 2) o.gp[l][q][r] = host_cast(gp, tag);
+        o.gm[l][q][r] = host_cast(gm, tag);
+      }
+    }
+    for (int r = 0; r <= kDevMaxN / 2; ++r) {
+      double gc = 0.0;
+      if ((N & 1) && r < H) gc = (double)((long double)d.A[H * N + r] * ia);
+      if ((N & 1) && r == H) gc = (double)((long double)d.Lp[H] * ia);
+      o.gc[l][r] = host_cast(gc, tag);
+    }
+  }
   o.g1 = host_cast(d.g1, tag);
   o.hg1 = host_cast(0.5 * d.g1, tag);
   o.gamma = host_cast(d.gamma, tag);

@@ -242,48 +242,62 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
     for (int v = 0; v < kNS; ++v) R::st(Fm + ((e0 + es2) * 3 + l) * kNS * nf + rot_var(v, l) * nf + t, F[v]);
   }
   __syncthreads();  // the own -l traces are dead: Q takes their space
-  const int es = threadIdx.x / n, q = threadIdx.x % n;
-  if (es < ne) {
-    const int c[3] = {q % N, (q / N) % N, q / (N * N)};
-    T grad[kNQ];
-#pragma unroll
-    for (int l = 0; l < 3; ++l) {
-      const int qn = c[l];
+  if constexpr (std::is_same<T, double>::value) {
+    // FP64: one line (element, direction l, variable v, face point t) per
+    // item, in the pairwise form of OpsT::gs..gc: 27 FP64 operations for
+    // the 5 outputs of a line at p = 4, where per-point sums take 35.
+    constexpr int H = N / 2;
+    for (int i = threadIdx.x; i < ne * 3 * kNS * nf; i += NT) {
+      const int es2 = i / (3 * kNS * nf);
+      int r = i - es2 * 3 * kNS * nf;
+      const int l = r / (kNS * nf);
+      r -= l * kNS * nf;
+      const int v = r / nf, t = r - v * nf;
       const int st = stride_of<N>(l);
-      const int b = q - qn * st;
-      const int t = tangential<N>(l, c[0], c[1], c[2]);
-      T row[N];
+      const int p0 = face_point<N>(l, 0, t);
+      const T* x = sU + (es2 * kNS + v) * n + p0;
+      const T tp = sTp[((es2 * 3 + l) * kNS + v) * nf + t];
+      const T tm = sTm[((es2 * 3 + l) * kNS + v) * nf + t];
+      const T tdif = tp - tm, tsum = tp + tm;
+      T ev[H], od[H];
 #pragma unroll
-      for (int r = 0; r < N; ++r) row[r] = o.As[l][qn * N + r];
-      const T lp = o.Lps[l][qn], lm = o.Lms[l][qn];
+      for (int k = 0; k < H; ++k) {
+        const T a = x[k * st], b = x[(N - 1 - k) * st];
+        ev[k] = a + b;
+        od[k] = a - b;
+      }
+      T* gs_out = sQ + (es2 * kNQ + l * kNS + v) * n + p0;
+      auto* gq_out = Q + ((e0 + es2) * kNQ + l * kNS + v) * n + p0;
 #pragma unroll
-      for (int v = 0; v < kNS; ++v) {
-        const T* line = sU + (es * kNS + v) * n + b;
-        const T tp = sTp[((es * 3 + l) * kNS + v) * nf + t];
-        const T tm = sTm[((es * 3 + l) * kNS + v) * nf + t];
-        T g;
-        if constexpr (std::is_same<T, double>::value) {
-          // the lifts first, then the volume terms: seven FP64 operations
-          T acc = fma(-lm, tm, lp * tp);
+      for (int k = 0; k < H; ++k) {
+        T U = o.gs[l][k] * tdif;
 #pragma unroll
-          for (int r = 0; r < N; ++r) acc = fma(-row[r], line[r * st], acc);
-          g = acc;
-        } else {  // one compensated 7-term dot product
-          Acc<T> acc;
+        for (int j = 0; j < H; ++j) U = fma(-o.gp[l][k][j], od[j], U);
+        T V = o.gd[l][k] * tsum;
 #pragma unroll
-          for (int r = 0; r < N; ++r) acc.add(-row[r], line[r * st]);
-          acc.add(lp, tp);
-          acc.add(-lm, tm);
-          g = acc.get();
-        }
-        grad[l * kNS + v] = g;
-        sQ[(es * kNQ + l * kNS + v) * n + q] = g;
-        R::st(Q + ((e0 + es) * kNQ + l * kNS + v) * n + q, g);
+        for (int j = 0; j < H; ++j) V = fma(-o.gm[l][k][j], ev[j], V);
+        if constexpr ((N & 1) != 0) V = fma(-o.gm[l][k][H], x[H * st], V);
+        const T lo = U + V, hi = U - V;
+        gs_out[k * st] = lo;
+        gs_out[(N - 1 - k) * st] = hi;
+        R::st(gq_out + k * st, lo);
+        R::st(gq_out + (N - 1 - k) * st, hi);
+      }
+      if constexpr ((N & 1) != 0) {
+        T g = o.gc[l][H] * tdif;
+#pragma unroll
+        for (int j = 0; j < H; ++j) g = fma(-o.gc[l][j], od[j], g);
+        gs_out[H * st] = g;
+        R::st(gq_out + H * st, g);
       }
     }
-    if constexpr (std::is_same<T, double>::value) {
-      if (ens) {
-        // enstrophy density rho |curl v|^2 / 2 at this Gauss point
+    if (ens) {
+      __syncthreads();
+      // enstrophy density rho |curl v|^2 / 2 at each Gauss point
+      const int es = threadIdx.x / n, q = threadIdx.x % n;
+      if (es < ne) {
+        const int c[3] = {q % N, (q / N) % N, q / (N * N)};
+        const double* gq = sQ + es * kNQ * n + q;  // component k at gq[k * n]
         const double* u = sU + es * kNS * n + q;
         double ir = 1.0 / u[0];
         double vv[3] = {u[n] * ir, u[2 * n] * ir, u[3 * n] * ir};
@@ -291,10 +305,42 @@ __device__ __forceinline__ void grad_body(const typename Real<T>::S* __restrict_
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
-          for (int i = 0; i < 3; ++i) G[i][j] = (grad[j * kNS + 1 + i] - grad[j * kNS] * vv[i]) * ir;
+          for (int i = 0; i < 3; ++i) G[i][j] = (gq[(j * kNS + 1 + i) * n] - gq[j * kNS * n] * vv[i]) * ir;
         double wx = G[2][1] - G[1][2], wy = G[0][2] - G[2][0], wz = G[1][0] - G[0][1];
         double w3 = ops.w[c[0]] * ops.w[c[1]] * ops.w[c[2]];
         sE[es * n + q] = ops.J * w3 * 0.5 * u[0] * (wx * wx + wy * wy + wz * wz);
+      }
+    }
+  } else {
+    // FP32 pairs: one Gauss point per thread, each output one compensated
+    // 7-term dot product
+    const int es = threadIdx.x / n, q = threadIdx.x % n;
+    if (es < ne) {
+      const int c[3] = {q % N, (q / N) % N, q / (N * N)};
+#pragma unroll
+      for (int l = 0; l < 3; ++l) {
+        const int qn = c[l];
+        const int st = stride_of<N>(l);
+        const int b = q - qn * st;
+        const int t = tangential<N>(l, c[0], c[1], c[2]);
+        T row[N];
+#pragma unroll
+        for (int r = 0; r < N; ++r) row[r] = o.As[l][qn * N + r];
+        const T lp = o.Lps[l][qn], lm = o.Lms[l][qn];
+#pragma unroll
+        for (int v = 0; v < kNS; ++v) {
+          const T* line = sU + (es * kNS + v) * n + b;
+          const T tp = sTp[((es * 3 + l) * kNS + v) * nf + t];
+          const T tm = sTm[((es * 3 + l) * kNS + v) * nf + t];
+          Acc<T> acc;
+#pragma unroll
+          for (int r = 0; r < N; ++r) acc.add(-row[r], line[r * st]);
+          acc.add(lp, tp);
+          acc.add(-lm, tm);
+          const T g = acc.get();
+          sQ[(es * kNQ + l * kNS + v) * n + q] = g;
+          R::st(Q + ((e0 + es) * kNQ + l * kNS + v) * n + q, g);
+        }
       }
     }
   }
