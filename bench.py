@@ -50,11 +50,11 @@ BYTES_RHS = 8 * (5 + 15 + 5)     # read U, read q, write k / next stage
 # kernels at 24^3 p=4 (13,824 elements; DRAM traffic and instruction counts
 # grow in proportion to the element count): DRAM bytes read + written, and
 # FP64 floating-point operations executed (2 per DFMA, 1 per DMUL or DADD;
-# k_grad: 20,100 DFMA + 5,250 DMUL + 1,350 DADD; k_rhs: 27,925 + 5,450 +
+# k_grad: 13,350 DFMA + 5,250 DMUL + 5,100 DADD; k_rhs: 27,925 + 5,450 +
 # 2,650).
 NCU_PER_ELEMENT = {
-    ("grad", 5, "fp64"): {"dram_bytes": (154.009344e6 + 320.630272e6) / 13824, "fp64_flops": 46800.0,
-                          "fp64_pipe_ops": 20100.0 + 5250.0 + 1350.0},
+    ("grad", 5, "fp64"): {"dram_bytes": (153.860608e6 + 322.368512e6) / 13824, "fp64_flops": 37050.0,
+                          "fp64_pipe_ops": 13350.0 + 5250.0 + 5100.0},
     ("rhs", 5, "fp64"): {"dram_bytes": (649.355776e6 + 189.405952e6) / 13824, "fp64_flops": 63950.0,
                          "fp64_pipe_ops": 27925.0 + 5450.0 + 2650.0},
     ("grad", 5, "mixed"): {"dram_bytes": (152.870400e6 + 312.989952e6) / 13824},
