@@ -237,6 +237,16 @@ int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* s
  * (No reference counterpart: the reference divides and calls sqrt,
  * solver.cpp:1291-1372.) */
 int ldg_probe_recip(int device, const double* x, double* r, double* rs, long n);
+/* The 1-D factors of the element operators for order p (1..7), host only
+ * (no device needed): Gauss points x and weights w (N = p+1 each), the weak
+ * derivative A[q*N + r] = (w_r/w_q) L_q'(x_r) (N*N), and the face lifts
+ * Lp/Lm[q] = L_q(+-1)/w_q (N each), L_q the Lagrange polynomial of Gauss
+ * point q.  The step kernels apply them by sum factorisation, and the FP64
+ * gradient pass uses their symmetries (A skew-centrosymmetric, Lp the
+ * mirror of Lm).  These are the 1-D factors of the reference's Sels, Kels
+ * and Kels2D with its mass matrix (solver.cpp:74-192) in the Gauss-point
+ * basis. */
+int ldg_operators_1d(int p, double* x, double* w, double* A, double* Lp, double* Lm);
 /* Measures the gradient pass's volume contraction alone (the product the
  * reference evaluates as a dense DGEMM, solver.cpp:500, here the
  * sum-factorised 1-D products along each direction) on the solver's

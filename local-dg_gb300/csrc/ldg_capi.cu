@@ -1425,6 +1425,21 @@ int ldg_probe_fp64(int device, double* tflops, double* fma_per_sm_clk, double* s
 
 int ldg_probe_fp64_peak(int device, double* tflops) { return ldg_probe_fp64(device, tflops, nullptr, nullptr); }
 
+int ldg_operators_1d(int p, double* x, double* w, double* A, double* Lp, double* Lm) {
+  if (!x || !w || !A || !Lp || !Lm) return fail(LDG_ERR_INVALID, "null buffer");
+  Ops1D o;
+  if (!build_ops1d(p, &o)) return fail(LDG_ERR_INVALID, "order p outside 1..7");
+  const int N = o.N;
+  for (int i = 0; i < N; ++i) {
+    x[i] = o.x[i];
+    w[i] = o.w[i];
+    Lp[i] = o.Lp[i];
+    Lm[i] = o.Lm[i];
+  }
+  for (int i = 0; i < N * N; ++i) A[i] = o.A[i];
+  return LDG_OK;
+}
+
 int ldg_probe_recip(int device, const double* x, double* r, double* rs, long n) {
   if (n < 0 || (n > 0 && (!x || !r || !rs))) return fail(LDG_ERR_INVALID, "null buffer");
   if (n == 0) return LDG_OK;

@@ -146,6 +146,7 @@ SIGNATURES = {
     "ldg_probe_fp64_peak": (_i, [_i, _dp]),
     "ldg_probe_fp64": (_i, [_i, _dp, _dp, _dp]),
     "ldg_probe_recip": (_i, [_i, _vp, _vp, _vp, ctypes.c_long]),
+    "ldg_operators_1d": (_i, [_i, _vp, _vp, _vp, _vp, _vp]),
     "ldg_probe_contraction": (_i, [_vp, _i, _i, _dp, _dp]),
     "ldg_set_transfer_chunks": (_i, [_vp, _i]),
     "ldg_advance_host": (_i, [_vp, _vp, _vp, _i]),
@@ -220,6 +221,18 @@ def probe_fp64(device: int = 0) -> dict:
     t, r, m = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     _check(load().ldg_probe_fp64(device, ctypes.byref(t), ctypes.byref(r), ctypes.byref(m)), "ldg_probe_fp64")
     return {"tflops": t.value, "fma_per_sm_clk": r.value, "sm_mhz": m.value}
+
+
+def operators_1d(p: int) -> dict:
+    """The 1-D element operators of order p as the library builds them (host
+    only): Gauss points x, weights w, weak derivative A (N x N, A[q, r]) and
+    face lifts Lp, Lm."""
+    N = p + 1
+    out = {k: np.zeros(N) for k in ("x", "w", "Lp", "Lm")}
+    out["A"] = np.zeros((N, N))
+    _check(load().ldg_operators_1d(p, out["x"].ctypes.data, out["w"].ctypes.data, out["A"].ctypes.data,
+                                    out["Lp"].ctypes.data, out["Lm"].ctypes.data), "ldg_operators_1d")
+    return out
 
 
 def probe_recip(x, device: int = 0):
