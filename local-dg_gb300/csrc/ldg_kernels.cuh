@@ -21,11 +21,12 @@
 // tangential directions in increasing order (mesh.cpp:428-501).
 //
 // One CTA works on EPC elements with one thread per (element, Gauss
-// point); face work is spread over all threads.  The FP64 kernels are
-// FP64-pipe bound on GB300, so the layout choices minimise arithmetic:
-// traces are written once by the producer of a state and read (not
-// recomputed) by both neighbours, and the mass matrix inverse is folded
-// into the 1-D operators.
+// point); face work is spread over all threads, and the FP64 gradient
+// takes one line of Gauss points per item.  The FP64 kernels are FP64-pipe
+// bound on GB300, so the layout choices minimise arithmetic: traces are
+// written once by the producer of a state and read (not recomputed) by both
+// neighbours, the mass matrix inverse is folded into the 1-D operators, and
+// the face fluxes of every direction run one code path per warp.
 #pragma once
 #include <type_traits>
 
