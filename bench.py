@@ -172,7 +172,7 @@ def host_memory_bytes() -> int:
 def port_bytes(nx: int, p: int) -> int:
     """Host bytes of the dense port at nx^3 order p: its work arrays (23.4
     states: uCurr, the u and Du interpolants, 4 ks, Dus, the face gather
-    and the volume fluxes) plus the driver's u and k."""
+    and the volume fluxes) plus the caller's u and k."""
     return int((p + 1) ** 3 * 5 * nx ** 3 * 8 * 25.5)
 
 
